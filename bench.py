@@ -1,0 +1,350 @@
+#!/usr/bin/env python3
+"""Channelizer throughput benchmark (output Msamples/s).
+
+Workload (the 256-channel configuration of the benchmark spec): one 2^26-sample
+complex<float> stream at 61.44 MSps (512 seeded tones + noise), 256 output
+channels with decimation D in {8,16,25,40,64,125,160,320}, up-factor U in
+{1,2,3}, 12-64 taps per phase; every channel shifts one tone to DC and
+resamples by U/D.  One step = one streaming apply of the whole 2^26-sample
+block through all 256 channels (NCO shift + polyphase resampling, fused).
+
+Reported (one JSON line, rank 0):
+  value      Sum of channel output samples / s with the input already resident
+             in HBM (CUDA events on the launch stream, max over ranks).
+  e2e        The same metric through the C ABI's host-buffer call
+             (fdsp_channelizer_apply_host): pinned host input -> H2D -> kernels
+             -> D2H of every output sample, per step.
+  roofline   Dominant kernel (the fused shift+resample kernel) against the
+             measured HBM copy bandwidth: algorithmic bytes per launch
+             (8 B per input sample + 8 B per output sample) / launch time.
+  cpu_baseline  The reference CPU channelizer path (oracle/_ref when built from
+             the reference sources, else the oracle's C restatement) on a
+             bounded sample of the same workload, channels spread over host
+             threads.
+Multi-GPU: replicas only -- every rank runs the same workload on its own GPU,
+with no collective on the data path; value sums ranks.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("channelizer_256: 2^26 complex64 @ 61.44 MSps, 512 tones + noise, 256 channels, "
+            "D in {8,16,25,40,64,125,160,320}, U in {1,2,3}, 12-64 taps/phase, Kaiser sinc")
+SEED = 2026
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 26, help="input samples per step (profiling uses smaller)")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=1 << 20, help="input samples of the CPU baseline sample")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons while the
+    timed region runs."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.rows = []
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if gpu_id:
+            cmd += ["-i", gpu_id]
+        try:
+            self.p = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        self.t = threading.Thread(target=self._read, daemon=True)
+        if self.p:
+            self.t.start()
+
+    def _read(self):
+        for line in self.p.stdout:
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if re.match(r"^[0-9.]+$", r[0])]
+        mx = [float(r[1]) for r in self.rows if re.match(r"^[0-9.]+$", r[1])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# --------------------------------------------------------------------------- helpers
+def peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(name: str, n_in: int):
+    """DRAM bytes per launch from the committed ncu summary of this kernel and
+    workload (profiles/<name>.md, line 'dram_bytes_per_input_sample: X'),
+    scaled to n_in input samples; None when no capture was summarised."""
+    p = os.path.join(ROOT, "profiles", f"{name}.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"dram_bytes_per_input_sample:\s*([0-9.eE+-]+)", open(p).read())
+    return float(m.group(1)) * n_in if m else None
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_channelizer_rate(fs, chans, x, threads, use_reference: bool) -> tuple[float, str, int]:
+    """Output Msamples/s of the reference CPU channelizer path on sample x,
+    channels split over `threads` host threads (ctypes releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+    threads = max(1, min(threads, len(chans)))
+    groups = [list(range(i, len(chans), threads)) for i in range(threads)]
+    if use_reference:
+        objs = [O.RefChannelizer(fs, [chans[i] for i in g]) for g in groups]
+        kind = "reference"
+    else:
+        objs = [O.Channelizer(fs, [chans[i] for i in g]) for g in groups]
+        kind = "port"
+
+    def work(o):
+        return sum(y.size for y in o.apply(x))
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        tot = sum(ex.map(work, objs))
+    dt = time.perf_counter() - t0
+    return tot / dt / 1e6, kind, threads
+
+
+# --------------------------------------------------------------------------- reference arm
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from libfalcon_dsp_gb300.workloads import channelizer_256_cpu_sample
+    from oracle import oracle as O
+    O.build()
+    n = args.cpu_sample // 4
+    x, fs, chans = channelizer_256_cpu_sample(n, args.n, SEED)
+    use_ref = O.have_reference()
+    threads = cpu_threads()
+    for _ in range(max(args.warmup, 0)):
+        cpu_channelizer_rate(fs, chans, x, threads, use_ref)
+    rates = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, kind, used = cpu_channelizer_rate(fs, chans, x, threads, use_ref)
+        rates.append(r)
+    wall = time.perf_counter() - t0
+    value = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": "channelizer output Msamples/s", "value": value, "unit": "Msamples/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": f"{n} input samples per step x 256 channels", "seed": SEED},
+        "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": used, "kind": kind,
+                         "sample": f"{n} input samples x 256 channels per step"},
+        "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- our arm
+def run_ours(args) -> None:
+    import torch
+    import torch.distributed as dist
+
+    import libfalcon_dsp_gb300 as F
+    from libfalcon_dsp_gb300 import _capi
+    from libfalcon_dsp_gb300.workloads import algorithmic_bytes, channelizer_256
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    x, fs, chans = channelizer_256(args.n, SEED, device=dev)
+    ch = F.MultiRateChannelizerCuda(fs, chans)
+    nch = len(chans)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    # outputs sized for the largest per-step count (counts vary by <= 1 between steps)
+    caps = [c + 2 for c in ch.out_count(x.numel())]
+    outs = [torch.empty(c, dtype=torch.complex64, device=dev) for c in caps]
+    optr = (C.c_void_p * nch)(*[o.data_ptr() for o in outs])
+    cap_arr = (C.c_uint64 * nch)(*caps)
+    n_out = (C.c_uint64 * nch)()
+    lib = _capi.lib()
+    xp = C.c_void_p(x.data_ptr())
+    torch.cuda.synchronize()
+
+    def step():
+        st = lib.fdsp_channelizer_apply(ch._h, xp, x.numel(), optr, cap_arr, n_out, C.c_void_p(sh))
+        if st != 0:
+            raise F.FdspError("fdsp_channelizer_apply", st, lib.fdsp_last_cuda_error())
+        return sum(n_out)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    gpu_id = None
+    try:
+        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    clocks = ClockSampler(gpu_id)
+    time.sleep(0.3)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    outputs = 0
+    for _ in range(args.steps):
+        outputs += step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        o = torch.tensor([float(outputs)], device=dev, dtype=torch.float64)
+        dist.all_reduce(o)
+        outputs_all = float(o.item())
+    else:
+        outputs_all = float(outputs)
+    ms_per_step = ms / args.steps
+    value = outputs_all / (ms / 1e3) / 1e6
+
+    # roofline of the fused kernel (the hist-update launch per step moves < 1 KB)
+    bytes_per_launch = algorithmic_bytes(x.numel(), outputs // args.steps)
+    achieved_gbs = bytes_per_launch / (ms_per_step / 1e3) / 1e9
+    pk = peaks()
+    traffic = ncu_traffic("poly_fp32_kernel_channelizer_256", x.numel())
+    roof = {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved_gbs / pk["hbm_gbs"], 4), "traffic": traffic,
+            "kernel": "poly_fp32_kernel", "peak_source": pk["source"],
+            "bytes_per_launch": bytes_per_launch}
+
+    # end to end through the host-buffer C ABI call (pinned host memory)
+    e2e = None
+    if not args.no_e2e:
+        hin = torch.empty(x.numel(), dtype=torch.complex64, pin_memory=True)
+        hin.copy_(x.cpu())
+        houts = [torch.empty(c, dtype=torch.complex64, pin_memory=True) for c in caps]
+        hptr = (C.c_void_p * nch)(*[h.data_ptr() for h in houts])
+        ch.reset_state()
+
+        def step_host():
+            st = lib.fdsp_channelizer_apply_host(ch._h, C.c_void_p(hin.data_ptr()), hin.numel(), hptr, cap_arr,
+                                                 n_out, C.c_void_p(sh))
+            if st != 0:
+                raise F.FdspError("fdsp_channelizer_apply_host", st, lib.fdsp_last_cuda_error())
+            return sum(n_out)
+
+        step_host()  # warm-up: allocates the library's device staging buffers
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eo = 0
+        for _ in range(args.e2e_steps):
+            eo += step_host()
+        dt = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([dt], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+            o = torch.tensor([float(eo)], device=dev, dtype=torch.float64)
+            dist.all_reduce(o)
+            eo = float(o.item())
+        e2e = {"value": eo / dt / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 8 * hin.numel(),
+               "d2h_bytes_per_step": 8 * (eo // args.e2e_steps if world == 1 else int(eo / world) // args.e2e_steps),
+               "steps": args.e2e_steps, "ms_per_step": 1000 * dt / args.e2e_steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build(with_reference=None)
+        n_s = min(args.cpu_sample, x.numel())
+        xs = x[:n_s].cpu().numpy()
+        rate, kind, used = cpu_channelizer_rate(fs, chans, xs, cpu_threads(), O.have_reference())
+        cpu = {"value": round(rate, 3), "unit": "Msamples/s", "cores": used, "kind": kind,
+               "sample": f"first {n_s} input samples of the workload x 256 channels, channels over {used} threads"}
+
+    if rank == 0:
+        line = {
+            "metric": "channelizer output Msamples/s", "value": round(value, 1), "unit": "Msamples/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_in": x.numel(), "channels": nch, "seed": SEED, "path": "plain FP32",
+                       "l2": "no flush: each step reads 512 MiB and writes ~9.6 GB, far above the 129 MB L2",
+                       "parallelism": f"replicas x{world}"},
+            "gpu_launches": 2 * args.steps,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,209 @@
+/*
+ * fdsp_c.h -- C ABI of libfalcon_dsp_gb300, the GB300 (sm_103a) implementation
+ * of libfalcon_dsp's multi-rate channelizer path.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: FDSP_OK (0) or a negative
+ *     fdsp_status code.  Nothing here prints or calls exit(); the reference's
+ *     convention of gpuAssert -> exit(code)
+ *     (src/utilities/falcon_dsp_cuda_utils.cu:84-94) is replaced by codes.
+ *   - Complex samples are fdsp_cf32 {re, im}: the memory layout of
+ *     std::complex<float>, cuFloatComplex and float2.
+ *   - *_apply functions take DEVICE pointers and a CUDA stream, enqueue their
+ *     kernels on that stream and return without synchronising.  All streaming
+ *     state (filter history, NCO counter, resampler phase and offset) lives
+ *     in the handle and on the device, so consecutive applies on one stream
+ *     continue the stream exactly as the reference's apply/apply/... does.
+ *   - *_apply_host functions take HOST pointers (pinned or pageable) and do
+ *     the host->device copy, the kernels and the device->host copy on the
+ *     given stream, then synchronise it: the drop-in for the reference's
+ *     std::vector in / std::vector out apply().
+ *   - Output counts are computed on the host with exact integer arithmetic
+ *     and equal, sample for sample, what the reference CPU loop emits
+ *     (src/transform/falcon_dsp_polyphase_resampler.cc:256-319).
+ *   - A handle is not thread safe; use one per host thread (the reference's
+ *     per-object mutex never locked anything, see
+ *     src/transform/falcon_dsp_polyphase_resampler.cc:258).
+ */
+#ifndef FDSP_C_H
+#define FDSP_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *fdsp_stream_t; /* same type as cudaStream_t; NULL = legacy default stream */
+
+typedef struct {
+    float re;
+    float im;
+} fdsp_cf32;
+
+enum fdsp_status {
+    FDSP_OK = 0,
+    FDSP_ERR_INVALID_ARG = -1,     /* bad pointer, size or configuration */
+    FDSP_ERR_NOT_INITIALIZED = -2, /* NULL handle */
+    FDSP_ERR_ALLOC = -3,           /* host or device allocation failed */
+    FDSP_ERR_CUDA = -4,            /* a CUDA runtime call failed; see fdsp_last_cuda_error() */
+    FDSP_ERR_CAPACITY = -5,        /* an output buffer is smaller than the output count */
+    FDSP_ERR_UNSUPPORTED = -6,     /* configuration outside this build's limits */
+    FDSP_ERR_NO_DEVICE = -7        /* no CUDA device is visible */
+};
+
+/* Short text for a status code (static storage). */
+const char *fdsp_status_string(int status);
+/* cudaError_t value behind the last FDSP_ERR_CUDA returned on this thread. */
+int fdsp_last_cuda_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int fdsp_version(void);
+
+/* ------------------------------------------------------------------------
+ * Helpers (host only, no GPU needed)
+ * ---------------------------------------------------------------------- */
+
+/* Replaces falcon_dsp_freq_shift::get_freq_shift_params
+ * (src/transform/falcon_dsp_freq_shift.cc:194-235): rollover index R and
+ * angular frequency omega of a shift of f Hz at fs samples/s. */
+int fdsp_freq_shift_params(uint32_t fs, int32_t f, uint32_t *rollover, double *omega);
+
+/* Replaces falcon_dsp::rat_approx (src/utilities/falcon_dsp_utils.cc:231-294). */
+int fdsp_rat_approx(double f, int64_t max_denom, int64_t *num, int64_t *den);
+
+/* Index bookkeeping of one resampler apply, in closed form: for n_in inputs
+ * from state (phase, x_offset), the number of outputs the reference loop
+ * emits and the state it leaves (the recurrence of
+ * src/transform/falcon_dsp_polyphase_resampler.cc:267-312).  Host only. */
+int fdsp_polyphase_advance(uint32_t up_rate, uint32_t down_rate, uint32_t phase, uint64_t x_offset, uint64_t n_in,
+                           uint64_t *n_out, uint32_t *phase_out, uint64_t *x_offset_out);
+
+/* ------------------------------------------------------------------------
+ * Multi-rate channelizer: per channel NCO shift then polyphase resampling,
+ * fused in one kernel launch over all channels.
+ * Replaces falcon_dsp_multi_rate_channelizer_cuda
+ * (hdr/transform/falcon_dsp_multi_rate_channelizer_cuda.h:73-167,
+ *  src/transform/falcon_dsp_multi_rate_channelizer_cuda.cu:87-576) and its
+ * CPU twin (hdr/transform/falcon_dsp_multi_rate_channelizer.h:70-134).
+ * ---------------------------------------------------------------------- */
+
+/* Field for field multi_rate_channelizer_channel_s
+ * (hdr/transform/falcon_dsp_multi_rate_channelizer.h:70-77), with the tap
+ * vector as a host pointer + count. */
+typedef struct {
+    uint32_t output_sample_rate_in_sps; /* informational, as in the reference */
+    int64_t freq_shift_in_hz;           /* truncated to int32 like the reference's NCO */
+    uint32_t up_rate;
+    uint32_t down_rate;
+    const fdsp_cf32 *resample_filter_coeffs; /* host pointer; only the real parts are used */
+    uint32_t num_coeffs;
+} fdsp_channel_cfg;
+
+typedef struct fdsp_channelizer fdsp_channelizer;
+
+/* initialize(input_sample_rate, channels)
+ * (src/transform/falcon_dsp_multi_rate_channelizer_cuda.cu:320-372). */
+int fdsp_channelizer_create(uint32_t input_sample_rate, const fdsp_channel_cfg *channels, uint32_t num_channels,
+                            fdsp_channelizer **out);
+int fdsp_channelizer_destroy(fdsp_channelizer *h);
+/* reset_state() (src/transform/falcon_dsp_multi_rate_channelizer.cc:166-173). */
+int fdsp_channelizer_reset(fdsp_channelizer *h);
+int fdsp_channelizer_num_channels(const fdsp_channelizer *h, uint32_t *n);
+/* Output count of every channel for the next block of n_in samples. */
+int fdsp_channelizer_out_count(const fdsp_channelizer *h, uint64_t n_in, uint64_t *n_out);
+/* apply(in, out) on device buffers: d_out[c] (capacity out_cap[c], may be
+ * NULL to skip the check) receives n_out[c] samples. */
+int fdsp_channelizer_apply(fdsp_channelizer *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *const *d_out,
+                           const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);
+/* apply(in, out) on host buffers (copies in, computes, copies out, syncs). */
+int fdsp_channelizer_apply_host(fdsp_channelizer *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,
+                                const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Polyphase resampler (single channel, no shift).
+ * Replaces falcon_dsp_polyphase_resampler_cuda
+ * (hdr/transform/falcon_dsp_polyphase_resampler_cuda.h:187-226) and the CPU
+ * class it derives from (hdr/transform/falcon_dsp_polyphase_resampler.h:168-195).
+ * Semantics are the CPU loop's (carried xOffset and phase across blocks).
+ * ---------------------------------------------------------------------- */
+typedef struct fdsp_resampler fdsp_resampler;
+
+int fdsp_resampler_create(uint32_t up_rate, uint32_t down_rate, const fdsp_cf32 *coeffs, uint32_t num_coeffs,
+                          fdsp_resampler **out);
+int fdsp_resampler_destroy(fdsp_resampler *h);
+int fdsp_resampler_reset(fdsp_resampler *h);
+/* coeffs_per_phase() (hdr/transform/falcon_dsp_polyphase_resampler.h:185). */
+int fdsp_resampler_coeffs_per_phase(const fdsp_resampler *h, uint32_t *cpp);
+/* Exact output count of the next apply of n_in samples. */
+int fdsp_resampler_out_count(const fdsp_resampler *h, uint64_t n_in, uint64_t *n_out);
+/* needed_out_count() exactly as the reference computes it
+ * (src/transform/falcon_dsp_polyphase_resampler.cc:204-228). */
+int fdsp_resampler_needed_out_count(const fdsp_resampler *h, uint32_t n_in, uint32_t *n_out);
+/* Current (coeff_phase, xOffset) streaming state. */
+int fdsp_resampler_state(const fdsp_resampler *h, uint32_t *coeff_phase, uint64_t *x_offset);
+int fdsp_resampler_apply(fdsp_resampler *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *d_out, uint64_t out_cap,
+                         uint64_t *n_out, fdsp_stream_t stream);
+int fdsp_resampler_apply_host(fdsp_resampler *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *h_out,
+                              uint64_t out_cap, uint64_t *n_out, fdsp_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * NCO frequency shift, one or many channels over one input.
+ * Replaces falcon_dsp_freq_shift_cuda (hdr/transform/falcon_dsp_freq_shift_cuda.h:187-212,
+ * src/transform/falcon_dsp_freq_shift_cuda.cu:275-488) and the CPU class
+ * (hdr/transform/falcon_dsp_freq_shift.h:84-121).
+ * ---------------------------------------------------------------------- */
+typedef struct fdsp_freq_shift fdsp_freq_shift;
+
+int fdsp_freq_shift_create(uint32_t input_sample_rate, const int32_t *shifts_hz, uint32_t num_channels,
+                           fdsp_freq_shift **out);
+int fdsp_freq_shift_destroy(fdsp_freq_shift *h);
+int fdsp_freq_shift_reset(fdsp_freq_shift *h);
+int fdsp_freq_shift_num_channels(const fdsp_freq_shift *h, uint32_t *n);
+/* Rollover-reduced sample counter of channel c (the reference's
+ * m_samples_handled / num_samples_handled). */
+int fdsp_freq_shift_counter(const fdsp_freq_shift *h, uint32_t c, uint64_t *counter);
+/* d_out[c] receives n_in shifted samples for each channel c. */
+int fdsp_freq_shift_apply(fdsp_freq_shift *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *const *d_out,
+                          fdsp_stream_t stream);
+int fdsp_freq_shift_apply_host(fdsp_freq_shift *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,
+                               fdsp_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * FIR filter with complex taps, output length = input length.
+ * Replaces falcon_dsp_fir_filter_cuda (hdr/transform/falcon_dsp_fir_filter_cuda.h:113-138,
+ * src/transform/falcon_dsp_fir_filter_cuda.cu:102-373) and the CPU class
+ * (hdr/transform/falcon_dsp_fir_filter.h:119-140).
+ * ---------------------------------------------------------------------- */
+typedef struct fdsp_fir fdsp_fir;
+
+int fdsp_fir_create(const fdsp_cf32 *coeffs, uint32_t num_coeffs, fdsp_fir **out);
+int fdsp_fir_destroy(fdsp_fir *h);
+int fdsp_fir_reset(fdsp_fir *h);
+int fdsp_fir_apply(fdsp_fir *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *d_out, fdsp_stream_t stream);
+int fdsp_fir_apply_host(fdsp_fir *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *h_out, fdsp_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Polar discriminator (FM demodulation core): out[n] = arg(x[n] conj(x[n-1])).
+ * Replaces falcon_dsp_polar_discriminator
+ * (hdr/transform/falcon_dsp_polar_discriminator.h:97-114,
+ *  src/transform/falcon_dsp_polar_discriminator.cc:134-171), which has no
+ * CUDA version in the reference.  The first apply after create/reset emits
+ * n_in - 1 values, later ones n_in.
+ * ---------------------------------------------------------------------- */
+typedef struct fdsp_polar fdsp_polar;
+
+int fdsp_polar_create(fdsp_polar **out);
+int fdsp_polar_destroy(fdsp_polar *h);
+int fdsp_polar_reset(fdsp_polar *h);
+int fdsp_polar_out_count(const fdsp_polar *h, uint64_t n_in, uint64_t *n_out);
+int fdsp_polar_apply(fdsp_polar *h, const fdsp_cf32 *d_in, uint64_t n_in, float *d_out, uint64_t *n_out,
+                     fdsp_stream_t stream);
+int fdsp_polar_apply_host(fdsp_polar *h, const fdsp_cf32 *h_in, uint64_t n_in, float *h_out, uint64_t *n_out,
+                          fdsp_stream_t stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* FDSP_C_H */

@@ -1,0 +1,390 @@
+"""libfalcon_dsp_gb300 -- GB300-native implementation of libfalcon_dsp's
+multi-rate channelizer path (NCO shift -> polyphase resampling -> FIR / FM
+demodulation), exposed with the reference's class interface.
+
+Each class mirrors one reference class (same name in the reference's
+``falcon_dsp`` namespace, same ``initialize / apply / reset_state`` streaming
+semantics) and calls the C ABI of ``_lib/libfalcon_dsp_gb300.so``:
+
+==============================  ==================================================
+Python class                    reference class (hdr/...)
+==============================  ==================================================
+``FreqShiftCuda``               transform/falcon_dsp_freq_shift_cuda.h:187-212
+``PolyphaseResamplerCuda``      transform/falcon_dsp_polyphase_resampler_cuda.h:187-226
+``MultiRateChannelizerCuda``    transform/falcon_dsp_multi_rate_channelizer_cuda.h:94-167
+``FirFilterCuda``               transform/falcon_dsp_fir_filter_cuda.h:113-138
+``PolarDiscriminatorCuda``      transform/falcon_dsp_polar_discriminator.h:97-114 (CPU-only there)
+==============================  ==================================================
+
+``apply`` accepts numpy arrays (host buffers; copied in and out like the
+reference's std::vector apply) or CUDA ``torch.Tensor`` of complex64 (device
+buffers; enqueued on the current torch stream, results returned as tensors).
+A failing call raises ``FdspError``; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import FdspError, cf32, channel_cfg
+
+__all__ = [
+    "FdspError", "FreqShiftCuda", "PolyphaseResamplerCuda", "MultiRateChannelizerCuda", "FirFilterCuda",
+    "PolarDiscriminatorCuda", "freq_shift_params", "rat_approx", "freq_shift_cuda", "resample_cuda",
+    "upfirdn_cuda", "fir_filter_cuda", "polar_discriminator_cuda", "channel",
+]
+
+
+def _is_tensor(x) -> bool:
+    return type(x).__module__.startswith("torch") and hasattr(x, "is_cuda")
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_handle() -> int:
+    torch = _torch()
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _c64(x) -> np.ndarray:
+    a = np.asarray(x)
+    if a.dtype == np.int16 and a.ndim == 2 and a.shape[-1] == 2:  # interleaved int16 pairs
+        a = a[:, 0].astype(np.float32) + 1j * a[:, 1].astype(np.float32)
+    return np.ascontiguousarray(a, dtype=np.complex64).reshape(-1)
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data) if a.size else C.c_void_p(0)
+
+
+def _tptr(t) -> C.c_void_p:
+    return C.c_void_p(t.data_ptr())
+
+
+def _dev_c64(t):
+    torch = _torch()
+    if t.dtype != torch.complex64:
+        raise TypeError("device input must be a complex64 CUDA tensor")
+    return t.contiguous().reshape(-1)
+
+
+def freq_shift_params(fs: int, f: int) -> tuple[int, float]:
+    """get_freq_shift_params (src/transform/falcon_dsp_freq_shift.cc:194-235)."""
+    r, w = C.c_uint32(), C.c_double()
+    _capi.call("fdsp_freq_shift_params", fs, int(np.int32(f)), C.byref(r), C.byref(w))
+    return r.value, w.value
+
+
+def rat_approx(f: float, max_denom: int) -> tuple[int, int]:
+    """rat_approx (src/utilities/falcon_dsp_utils.cc:231-294)."""
+    n, d = C.c_int64(), C.c_int64()
+    _capi.call("fdsp_rat_approx", float(f), int(max_denom), C.byref(n), C.byref(d))
+    return n.value, d.value
+
+
+def channel(output_sample_rate_in_sps: int, freq_shift_in_hz: int, up_rate: int, down_rate: int,
+            resample_filter_coeffs) -> dict:
+    """multi_rate_channelizer_channel_s
+    (hdr/transform/falcon_dsp_multi_rate_channelizer.h:70-77) as a dict."""
+    return dict(output_sample_rate_in_sps=int(output_sample_rate_in_sps), freq_shift_in_hz=int(freq_shift_in_hz),
+                up_rate=int(up_rate), down_rate=int(down_rate), coeffs=_c64(resample_filter_coeffs))
+
+
+class _Handle:
+    _destroy = ""
+
+    def __init__(self):
+        self._h = C.c_void_p(0)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                getattr(_capi.lib(), self._destroy)(h)
+            except Exception:
+                pass
+            self._h = C.c_void_p(0)
+
+
+class MultiRateChannelizerCuda(_Handle):
+    """falcon_dsp_multi_rate_channelizer_cuda: per channel NCO shift, then
+    polyphase up/down resampling, all channels fused in one launch."""
+    _destroy = "fdsp_channelizer_destroy"
+
+    def __init__(self, input_sample_rate: int | None = None, channels=None):
+        super().__init__()
+        self.initialized = False
+        if input_sample_rate is not None and channels is not None:
+            if not self.initialize(input_sample_rate, channels):
+                raise FdspError("fdsp_channelizer_create", -1)
+
+    def initialize(self, input_sample_rate: int, channels) -> bool:
+        if self.initialized or input_sample_rate == 0 or len(channels) == 0:
+            return False
+        self._keep = []
+        arr = (channel_cfg * len(channels))()
+        for i, ch in enumerate(channels):
+            taps = _c64(ch["coeffs"] if "coeffs" in ch else ch["resample_filter_coeffs"])
+            self._keep.append(taps)
+            arr[i].output_sample_rate_in_sps = int(ch.get("output_sample_rate_in_sps", 0))
+            arr[i].freq_shift_in_hz = int(ch["freq_shift_in_hz"])
+            arr[i].up_rate = int(ch["up_rate"])
+            arr[i].down_rate = int(ch["down_rate"])
+            arr[i].resample_filter_coeffs = taps.ctypes.data
+            arr[i].num_coeffs = taps.size
+        _capi.call("fdsp_channelizer_create", int(input_sample_rate), arr, len(channels), C.byref(self._h))
+        self.num_channels = len(channels)
+        self.initialized = True
+        return True
+
+    def out_count(self, n_in: int) -> list[int]:
+        out = (C.c_uint64 * self.num_channels)()
+        _capi.call("fdsp_channelizer_out_count", self._h, int(n_in), out)
+        return list(out)
+
+    def reset_state(self) -> None:
+        _capi.call("fdsp_channelizer_reset", self._h)
+
+    def apply(self, x, out=None, stream: int | None = None):
+        if _is_tensor(x):
+            return self._apply_device(x, out, stream)
+        x = _c64(x)
+        cnt = self.out_count(x.size)
+        outs = [np.empty(max(c, 1), np.complex64) for c in cnt]
+        optr = (C.c_void_p * self.num_channels)(*[o.ctypes.data for o in outs])
+        n_out = (C.c_uint64 * self.num_channels)()
+        _capi.call("fdsp_channelizer_apply_host", self._h, _ptr(x), x.size, optr, None, n_out,
+                   C.c_void_p(stream or 0))
+        return [o[: n_out[i]] for i, o in enumerate(outs)]
+
+    def _apply_device(self, x, out, stream):
+        torch = _torch()
+        x = _dev_c64(x)
+        cnt = self.out_count(x.numel())
+        if out is None:
+            out = [torch.empty(max(c, 1), dtype=torch.complex64, device=x.device) for c in cnt]
+        optr = (C.c_void_p * self.num_channels)(*[o.data_ptr() for o in out])
+        cap = (C.c_uint64 * self.num_channels)(*[o.numel() for o in out])
+        n_out = (C.c_uint64 * self.num_channels)()
+        s = _stream_handle() if stream is None else stream
+        _capi.call("fdsp_channelizer_apply", self._h, _tptr(x), x.numel(), optr, cap, n_out, C.c_void_p(s))
+        return [o[: n_out[i]] for i, o in enumerate(out)]
+
+
+class PolyphaseResamplerCuda(_Handle):
+    """falcon_dsp_polyphase_resampler_cuda with the CPU class's streaming
+    semantics (carried phase and xOffset; only the taps' real parts used)."""
+    _destroy = "fdsp_resampler_destroy"
+
+    def __init__(self, up_rate: int | None = None, down_rate: int | None = None, coeffs=None):
+        super().__init__()
+        self.initialized = False
+        if up_rate is not None:
+            if not self.initialize(up_rate, down_rate, coeffs):
+                raise FdspError("fdsp_resampler_create", -1)
+
+    def initialize(self, up_rate: int, down_rate: int, coeffs) -> bool:
+        if self.initialized:
+            return False
+        taps = _c64(coeffs)
+        _capi.call("fdsp_resampler_create", int(up_rate), int(down_rate), _ptr(taps), taps.size, C.byref(self._h))
+        self.initialized = True
+        return True
+
+    def reset_state(self) -> None:
+        _capi.call("fdsp_resampler_reset", self._h)
+
+    def coeffs_per_phase(self) -> int:
+        v = C.c_uint32()
+        _capi.call("fdsp_resampler_coeffs_per_phase", self._h, C.byref(v))
+        return v.value
+
+    def needed_out_count(self, n_in: int) -> int:
+        v = C.c_uint32()
+        _capi.call("fdsp_resampler_needed_out_count", self._h, int(n_in), C.byref(v))
+        return v.value
+
+    def out_count(self, n_in: int) -> int:
+        v = C.c_uint64()
+        _capi.call("fdsp_resampler_out_count", self._h, int(n_in), C.byref(v))
+        return v.value
+
+    def state(self) -> tuple[int, int]:
+        ph, xo = C.c_uint32(), C.c_uint64()
+        _capi.call("fdsp_resampler_state", self._h, C.byref(ph), C.byref(xo))
+        return ph.value, xo.value
+
+    def apply(self, x, out=None, stream: int | None = None):
+        if _is_tensor(x):
+            torch = _torch()
+            x = _dev_c64(x)
+            n = self.out_count(x.numel())
+            if out is None:
+                out = torch.empty(max(n, 1), dtype=torch.complex64, device=x.device)
+            got = C.c_uint64()
+            s = _stream_handle() if stream is None else stream
+            _capi.call("fdsp_resampler_apply", self._h, _tptr(x), x.numel(), _tptr(out), out.numel(),
+                       C.byref(got), C.c_void_p(s))
+            return out[: got.value]
+        real_in = np.isrealobj(x) and np.asarray(x).dtype != np.int16
+        xa = _c64(x)
+        n = self.out_count(xa.size)
+        y = np.empty(max(n, 1), np.complex64)
+        got = C.c_uint64()
+        _capi.call("fdsp_resampler_apply_host", self._h, _ptr(xa), xa.size, _ptr(y), y.size, C.byref(got),
+                   C.c_void_p(stream or 0))
+        y = y[: got.value]
+        return y.real.copy() if real_in else y  # apply(vector<float>) overload
+
+
+class FreqShiftCuda(_Handle):
+    """falcon_dsp_freq_shift_cuda: one or many NCO shifts of one input."""
+    _destroy = "fdsp_freq_shift_destroy"
+
+    def __init__(self, input_sample_rate: int | None = None, shifts=None):
+        super().__init__()
+        self.initialized = False
+        if input_sample_rate is not None:
+            if not self.initialize(input_sample_rate, shifts):
+                raise FdspError("fdsp_freq_shift_create", -1)
+
+    def initialize(self, input_sample_rate: int, shifts) -> bool:
+        if self.initialized:
+            return False
+        self.single = np.isscalar(shifts)
+        sh = np.atleast_1d(np.asarray(shifts, dtype=np.int64)).astype(np.int32)
+        arr = (C.c_int32 * sh.size)(*[int(v) for v in sh])
+        _capi.call("fdsp_freq_shift_create", int(input_sample_rate), arr, sh.size, C.byref(self._h))
+        self.num_channels = int(sh.size)
+        self.initialized = True
+        return True
+
+    def reset_state(self) -> None:
+        _capi.call("fdsp_freq_shift_reset", self._h)
+
+    def counter(self, c: int = 0) -> int:
+        v = C.c_uint64()
+        _capi.call("fdsp_freq_shift_counter", self._h, c, C.byref(v))
+        return v.value
+
+    def apply(self, x, out=None, stream: int | None = None):
+        if _is_tensor(x):
+            torch = _torch()
+            x = _dev_c64(x)
+            if out is None:
+                out = [torch.empty(max(x.numel(), 1), dtype=torch.complex64, device=x.device)
+                       for _ in range(self.num_channels)]
+            optr = (C.c_void_p * self.num_channels)(*[o.data_ptr() for o in out])
+            s = _stream_handle() if stream is None else stream
+            _capi.call("fdsp_freq_shift_apply", self._h, _tptr(x), x.numel(), optr, C.c_void_p(s))
+            res = [o[: x.numel()] for o in out]
+        else:
+            xa = _c64(x)
+            res = [np.empty(max(xa.size, 1), np.complex64) for _ in range(self.num_channels)]
+            optr = (C.c_void_p * self.num_channels)(*[o.ctypes.data for o in res])
+            _capi.call("fdsp_freq_shift_apply_host", self._h, _ptr(xa), xa.size, optr, C.c_void_p(stream or 0))
+            res = [o[: xa.size] for o in res]
+        return res[0] if self.single else res
+
+
+class FirFilterCuda(_Handle):
+    """falcon_dsp_fir_filter_cuda: complex-tap FIR, output length = input
+    length, history carried across apply calls."""
+    _destroy = "fdsp_fir_destroy"
+
+    def __init__(self, coeffs):
+        super().__init__()
+        taps = _c64(coeffs)
+        _capi.call("fdsp_fir_create", _ptr(taps), taps.size, C.byref(self._h))
+
+    def reset_state(self) -> None:
+        _capi.call("fdsp_fir_reset", self._h)
+
+    def apply(self, x, out=None, stream: int | None = None):
+        if _is_tensor(x):
+            torch = _torch()
+            x = _dev_c64(x)
+            if out is None:
+                out = torch.empty(max(x.numel(), 1), dtype=torch.complex64, device=x.device)
+            s = _stream_handle() if stream is None else stream
+            _capi.call("fdsp_fir_apply", self._h, _tptr(x), x.numel(), _tptr(out), C.c_void_p(s))
+            return out[: x.numel()]
+        as_i16 = np.asarray(x).dtype == np.int16
+        xa = _c64(x)
+        y = np.empty(max(xa.size, 1), np.complex64)
+        _capi.call("fdsp_fir_apply_host", self._h, _ptr(xa), xa.size, _ptr(y), C.c_void_p(stream or 0))
+        y = y[: xa.size]
+        if as_i16:  # apply(vector<complex<int16_t>>): truncating cast back (fir_filter.cc:168-172)
+            out16 = np.empty((y.size, 2), np.int16)
+            out16[:, 0] = np.trunc(y.real).astype(np.int16)
+            out16[:, 1] = np.trunc(y.imag).astype(np.int16)
+            return out16
+        return y
+
+
+class PolarDiscriminatorCuda(_Handle):
+    """falcon_dsp_polar_discriminator on the GPU (the reference has only the
+    CPU class): out[n] = arg(x[n] * conj(x[n-1]))."""
+    _destroy = "fdsp_polar_destroy"
+
+    def __init__(self):
+        super().__init__()
+        _capi.call("fdsp_polar_create", C.byref(self._h))
+
+    def reset_state(self) -> None:
+        _capi.call("fdsp_polar_reset", self._h)
+
+    def apply(self, x, out=None, stream: int | None = None):
+        if _is_tensor(x):
+            torch = _torch()
+            x = _dev_c64(x)
+            if out is None:
+                out = torch.empty(max(x.numel(), 1), dtype=torch.float32, device=x.device)
+            got = C.c_uint64()
+            s = _stream_handle() if stream is None else stream
+            _capi.call("fdsp_polar_apply", self._h, _tptr(x), x.numel(), _tptr(out), C.byref(got), C.c_void_p(s))
+            return out[: got.value]
+        xa = _c64(x)
+        y = np.empty(max(xa.size, 1), np.float32)
+        got = C.c_uint64()
+        _capi.call("fdsp_polar_apply_host", self._h, _ptr(xa), xa.size, _ptr(y), C.byref(got),
+                   C.c_void_p(stream or 0))
+        return y[: got.value]
+
+
+# ---- free functions (one-shot), as in the reference headers ---------------
+def freq_shift_cuda(input_sample_rate: int, x, shift):
+    """freq_shift_cuda (src/transform/falcon_dsp_freq_shift_cuda.cu:90-119)."""
+    return FreqShiftCuda(input_sample_rate, shift).apply(x)
+
+
+def resample_cuda(input_sample_rate: int, x, coeffs, output_sample_rate: int):
+    """resample_cuda (src/transform/falcon_dsp_resample_cuda.cu:124-135):
+    up/down from rat_approx(fs_out/fs_in, 1024), then one apply."""
+    up, down = rat_approx(float(output_sample_rate) / float(input_sample_rate), 1024)
+    return PolyphaseResamplerCuda(up, down, coeffs).apply(x)
+
+
+upfirdn_cuda = resample_cuda
+
+
+def fir_filter_cuda(coeffs, x):
+    """fir_filter_cuda (src/transform/falcon_dsp_fir_filter_cuda.cu:86-97)."""
+    return FirFilterCuda(coeffs).apply(x)
+
+
+def polar_discriminator_cuda(x):
+    return PolarDiscriminatorCuda().apply(x)
+
+
+# Reference spellings of the class names.
+falcon_dsp_multi_rate_channelizer_cuda = MultiRateChannelizerCuda
+falcon_dsp_polyphase_resampler_cuda = PolyphaseResamplerCuda
+falcon_dsp_freq_shift_cuda = FreqShiftCuda
+falcon_dsp_fir_filter_cuda = FirFilterCuda
+falcon_dsp_polar_discriminator_cuda = PolarDiscriminatorCuda

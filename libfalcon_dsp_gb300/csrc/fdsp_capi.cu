@@ -1,0 +1,569 @@
+// The C ABI (include/fdsp_c.h): opaque handles over the polyphase engine and
+// the elementwise stages.  No entry point prints, throws across the boundary
+// or exits; every failure is a negative status code.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "fdsp_internal.h"
+#include "fdsp_shift_polar.h"
+
+namespace fdsp {
+
+static thread_local int g_last_cuda_error = 0;
+
+void set_last_cuda_error(int code) { g_last_cuda_error = code; }
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return FDSP_OK;
+  g_last_cuda_error = (int)e;
+  if (e == cudaErrorMemoryAllocation) return FDSP_ERR_ALLOC;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return FDSP_ERR_NO_DEVICE;
+  return FDSP_ERR_CUDA;
+}
+
+// Grow-only device buffer used by the *_apply_host entry points.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  int ensure(size_t want) {
+    if (want <= bytes) return FDSP_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) return cuda_status(e);
+    bytes = want;
+    return FDSP_OK;
+  }
+};
+
+}  // namespace fdsp
+
+using namespace fdsp;
+
+struct fdsp_channelizer {
+  PolyEngine eng;
+  DevBuf in;
+  std::vector<DevBuf> out;
+};
+
+struct fdsp_resampler {
+  PolyEngine eng;
+  uint32_t up = 1, down = 1;
+  DevBuf in, out;
+};
+
+struct fdsp_fir {
+  PolyEngine eng;
+  DevBuf in, out;
+};
+
+struct fdsp_freq_shift {
+  uint32_t fs = 0;
+  std::vector<NcoConst> nco;
+  NcoConst* d_nco = nullptr;
+  uint64_t abs0 = 0;
+  DevBuf in;
+  std::vector<DevBuf> out;
+  ~fdsp_freq_shift() {
+    if (d_nco) cudaFree(d_nco);
+  }
+};
+
+struct fdsp_polar {
+  float2* d_prev = nullptr;
+  bool have_prev = false;
+  DevBuf in, out;
+  ~fdsp_polar() {
+    if (d_prev) cudaFree(d_prev);
+  }
+};
+
+#define FDSP_TRY(expr)              \
+  do {                              \
+    int st_ = (expr);               \
+    if (st_ != FDSP_OK) return st_; \
+  } while (0)
+
+extern "C" {
+
+const char* fdsp_status_string(int status) {
+  switch (status) {
+    case FDSP_OK: return "ok";
+    case FDSP_ERR_INVALID_ARG: return "invalid argument";
+    case FDSP_ERR_NOT_INITIALIZED: return "handle not initialized";
+    case FDSP_ERR_ALLOC: return "allocation failed";
+    case FDSP_ERR_CUDA: return "CUDA runtime error";
+    case FDSP_ERR_CAPACITY: return "output buffer too small";
+    case FDSP_ERR_UNSUPPORTED: return "configuration outside this build's limits";
+    case FDSP_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+int fdsp_last_cuda_error(void) { return g_last_cuda_error; }
+
+int fdsp_version(void) { return 100; }
+
+int fdsp_freq_shift_params(uint32_t fs, int32_t f, uint32_t* rollover, double* omega) {
+  if (!rollover || !omega) return FDSP_ERR_INVALID_ARG;
+  // falcon_dsp_freq_shift.cc:194-235 (abs(0) gives an infinite ratio whose
+  // integer conversion is undefined in the reference; 0 is reported here)
+  double r = (double)fs / (double)std::llabs((long long)f);
+  while (r < 1e5) r *= 10.0;
+  *rollover = (f == 0) ? 0u : (uint32_t)std::round(r);
+  *omega = ((double)f / (double)fs) * 2.0 * M_PI;
+  return FDSP_OK;
+}
+
+int fdsp_rat_approx(double f, int64_t md, int64_t* num, int64_t* den) {
+  if (!num || !den) return FDSP_ERR_INVALID_ARG;
+  // Continued-fraction convergents with a denominator cap
+  // (falcon_dsp_utils.cc:231-294).
+  int64_t h[3] = {0, 1, 0}, k[3] = {1, 0, 0};
+  int64_t n = 1;
+  bool neg = false;
+  if (md <= 1) {
+    *den = 1;
+    *num = (int64_t)f;
+    return FDSP_OK;
+  }
+  if (f < 0) {
+    neg = true;
+    f = -f;
+  }
+  while (f != std::floor(f)) {
+    n <<= 1;
+    f *= 2;
+  }
+  int64_t d = (int64_t)f;
+  for (int i = 0; i < 64; i++) {
+    const int64_t a = n ? d / n : 0;
+    if (i && !a) break;
+    int64_t x = d;
+    d = n;
+    n = x % n;
+    x = a;
+    if (k[1] * a + k[0] >= md) {
+      x = (md - k[0]) / k[1];
+      if (x * 2 >= a || k[1] >= md)
+        i = 65;
+      else
+        break;
+    }
+    h[2] = x * h[1] + h[0];
+    h[0] = h[1];
+    h[1] = h[2];
+    k[2] = x * k[1] + k[0];
+    k[0] = k[1];
+    k[1] = k[2];
+  }
+  *den = k[1];
+  *num = neg ? -h[1] : h[1];
+  return FDSP_OK;
+}
+
+int fdsp_polyphase_advance(uint32_t up, uint32_t down, uint32_t phase, uint64_t xoffset, uint64_t n_in,
+                           uint64_t* n_out, uint32_t* phase_out, uint64_t* xoffset_out) {
+  if (up == 0 || down == 0 || phase >= up) return FDSP_ERR_INVALID_ARG;
+  const uint64_t M = polyphase_out_count(up, down, phase, xoffset, n_in);
+  polyphase_advance(up, down, phase, xoffset, n_in, M);
+  if (n_out) *n_out = M;
+  if (phase_out) *phase_out = phase;
+  if (xoffset_out) *xoffset_out = xoffset;
+  return FDSP_OK;
+}
+
+/* ---------------- channelizer ---------------- */
+int fdsp_channelizer_create(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, fdsp_channelizer** out) {
+  if (!out) return FDSP_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (fs == 0 || nch == 0 || !ch) return FDSP_ERR_INVALID_ARG;
+  fdsp_channelizer* h = new (std::nothrow) fdsp_channelizer();
+  if (!h) return FDSP_ERR_ALLOC;
+  int st = h->eng.init(fs, ch, nch, false);
+  if (st != FDSP_OK) {
+    delete h;
+    return st;
+  }
+  h->out.resize(nch);
+  *out = h;
+  return FDSP_OK;
+}
+
+int fdsp_channelizer_destroy(fdsp_channelizer* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  delete h;
+  return FDSP_OK;
+}
+
+int fdsp_channelizer_reset(fdsp_channelizer* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  h->eng.reset();
+  return FDSP_OK;
+}
+
+int fdsp_channelizer_num_channels(const fdsp_channelizer* h, uint32_t* n) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!n) return FDSP_ERR_INVALID_ARG;
+  *n = h->eng.num_channels();
+  return FDSP_OK;
+}
+
+int fdsp_channelizer_out_count(const fdsp_channelizer* h, uint64_t n_in, uint64_t* n_out) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return h->eng.out_counts(n_in, n_out);
+}
+
+int fdsp_channelizer_apply(fdsp_channelizer* h, const fdsp_cf32* d_in, uint64_t n_in, fdsp_cf32* const* d_out,
+                           const uint64_t* out_cap, uint64_t* n_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return h->eng.apply(reinterpret_cast<const float2*>(d_in), n_in, reinterpret_cast<float2* const*>(d_out), out_cap,
+                      n_out, (cudaStream_t)stream);
+}
+
+int fdsp_channelizer_apply_host(fdsp_channelizer* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* const* h_out,
+                                const uint64_t* out_cap, uint64_t* n_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if ((n_in > 0 && !h_in) || !n_out) return FDSP_ERR_INVALID_ARG;
+  const uint32_t nch = h->eng.num_channels();
+  std::vector<uint64_t> cnt(nch);
+  FDSP_TRY(h->eng.out_counts(n_in, cnt.data()));
+  for (uint32_t c = 0; c < nch; ++c) {
+    if (out_cap && out_cap[c] < cnt[c]) return FDSP_ERR_CAPACITY;
+    if (cnt[c] > 0 && (!h_out || !h_out[c])) return FDSP_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  FDSP_TRY(h->in.ensure(n_in * sizeof(float2) + 16));
+  std::vector<float2*> dptr(nch);
+  for (uint32_t c = 0; c < nch; ++c) {
+    FDSP_TRY(h->out[c].ensure(cnt[c] * sizeof(float2) + 16));
+    dptr[c] = static_cast<float2*>(h->out[c].p);
+  }
+  if (n_in) FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * sizeof(float2), cudaMemcpyHostToDevice, s)));
+  FDSP_TRY(h->eng.apply(static_cast<const float2*>(h->in.p), n_in, dptr.data(), nullptr, n_out, s));
+  for (uint32_t c = 0; c < nch; ++c) {
+    if (n_out[c])
+      FDSP_TRY(cuda_status(
+          cudaMemcpyAsync(h_out[c], dptr[c], n_out[c] * sizeof(float2), cudaMemcpyDeviceToHost, s)));
+  }
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+/* ---------------- resampler ---------------- */
+int fdsp_resampler_create(uint32_t up, uint32_t down, const fdsp_cf32* coeffs, uint32_t ncoeffs,
+                          fdsp_resampler** out) {
+  if (!out) return FDSP_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (up == 0 || down == 0 || !coeffs || ncoeffs == 0) return FDSP_ERR_INVALID_ARG;
+  fdsp_resampler* h = new (std::nothrow) fdsp_resampler();
+  if (!h) return FDSP_ERR_ALLOC;
+  fdsp_channel_cfg c;
+  c.output_sample_rate_in_sps = 0;
+  c.freq_shift_in_hz = 0;
+  c.up_rate = up;
+  c.down_rate = down;
+  c.resample_filter_coeffs = coeffs;
+  c.num_coeffs = ncoeffs;
+  int st = h->eng.init(1, &c, 1, false);
+  if (st != FDSP_OK) {
+    delete h;
+    return st;
+  }
+  h->up = up;
+  h->down = down;
+  *out = h;
+  return FDSP_OK;
+}
+
+int fdsp_resampler_destroy(fdsp_resampler* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  delete h;
+  return FDSP_OK;
+}
+
+int fdsp_resampler_reset(fdsp_resampler* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  h->eng.reset();
+  return FDSP_OK;
+}
+
+int fdsp_resampler_coeffs_per_phase(const fdsp_resampler* h, uint32_t* cpp) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!cpp) return FDSP_ERR_INVALID_ARG;
+  *cpp = h->eng.coeffs_per_phase(0);
+  return FDSP_OK;
+}
+
+int fdsp_resampler_out_count(const fdsp_resampler* h, uint64_t n_in, uint64_t* n_out) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return h->eng.out_counts(n_in, n_out);
+}
+
+int fdsp_resampler_needed_out_count(const fdsp_resampler* h, uint32_t n_in, uint32_t* n_out) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!n_out) return FDSP_ERR_INVALID_ARG;
+  // polyphase_resampler.cc:216-228, in its own uint32 arithmetic
+  const uint64_t np = (uint64_t)n_in * (uint64_t)h->up;
+  uint32_t need = (uint32_t)(np / h->down);
+  const uint32_t ph = h->eng.phase_of(0);
+  const uint32_t xo = (uint32_t)h->eng.xoffset_of(0);
+  if ((uint32_t)(ph + h->up * xo) < (np % h->down)) need++;
+  *n_out = need;
+  return FDSP_OK;
+}
+
+int fdsp_resampler_state(const fdsp_resampler* h, uint32_t* coeff_phase, uint64_t* x_offset) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (coeff_phase) *coeff_phase = h->eng.phase_of(0);
+  if (x_offset) *x_offset = h->eng.xoffset_of(0);
+  return FDSP_OK;
+}
+
+int fdsp_resampler_apply(fdsp_resampler* h, const fdsp_cf32* d_in, uint64_t n_in, fdsp_cf32* d_out,
+                         uint64_t out_cap, uint64_t* n_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  float2* o = reinterpret_cast<float2*>(d_out);
+  return h->eng.apply(reinterpret_cast<const float2*>(d_in), n_in, &o, &out_cap, n_out, (cudaStream_t)stream);
+}
+
+int fdsp_resampler_apply_host(fdsp_resampler* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* h_out,
+                              uint64_t out_cap, uint64_t* n_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if ((n_in > 0 && !h_in) || !n_out) return FDSP_ERR_INVALID_ARG;
+  uint64_t cnt = 0;
+  FDSP_TRY(h->eng.out_counts(n_in, &cnt));
+  if (out_cap < cnt) return FDSP_ERR_CAPACITY;
+  if (cnt > 0 && !h_out) return FDSP_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  FDSP_TRY(h->in.ensure(n_in * sizeof(float2) + 16));
+  FDSP_TRY(h->out.ensure(cnt * sizeof(float2) + 16));
+  if (n_in) FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * sizeof(float2), cudaMemcpyHostToDevice, s)));
+  float2* o = static_cast<float2*>(h->out.p);
+  FDSP_TRY(h->eng.apply(static_cast<const float2*>(h->in.p), n_in, &o, nullptr, n_out, s));
+  if (*n_out)
+    FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out, o, *n_out * sizeof(float2), cudaMemcpyDeviceToHost, s)));
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+/* ---------------- FIR ---------------- */
+int fdsp_fir_create(const fdsp_cf32* coeffs, uint32_t ncoeffs, fdsp_fir** out) {
+  if (!out) return FDSP_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (!coeffs || ncoeffs == 0) return FDSP_ERR_INVALID_ARG;
+  fdsp_fir* h = new (std::nothrow) fdsp_fir();
+  if (!h) return FDSP_ERR_ALLOC;
+  fdsp_channel_cfg c;
+  c.output_sample_rate_in_sps = 0;
+  c.freq_shift_in_hz = 0;
+  c.up_rate = 1;
+  c.down_rate = 1;
+  c.resample_filter_coeffs = coeffs;
+  c.num_coeffs = ncoeffs;
+  int st = h->eng.init(1, &c, 1, true);
+  if (st != FDSP_OK) {
+    delete h;
+    return st;
+  }
+  *out = h;
+  return FDSP_OK;
+}
+
+int fdsp_fir_destroy(fdsp_fir* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  delete h;
+  return FDSP_OK;
+}
+
+int fdsp_fir_reset(fdsp_fir* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  h->eng.reset();
+  return FDSP_OK;
+}
+
+int fdsp_fir_apply(fdsp_fir* h, const fdsp_cf32* d_in, uint64_t n_in, fdsp_cf32* d_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  float2* o = reinterpret_cast<float2*>(d_out);
+  uint64_t cnt = 0;
+  return h->eng.apply(reinterpret_cast<const float2*>(d_in), n_in, &o, nullptr, &cnt, (cudaStream_t)stream);
+}
+
+int fdsp_fir_apply_host(fdsp_fir* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* h_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (n_in > 0 && (!h_in || !h_out)) return FDSP_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  FDSP_TRY(h->in.ensure(n_in * sizeof(float2) + 16));
+  FDSP_TRY(h->out.ensure(n_in * sizeof(float2) + 16));
+  if (n_in) FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * sizeof(float2), cudaMemcpyHostToDevice, s)));
+  float2* o = static_cast<float2*>(h->out.p);
+  uint64_t cnt = 0;
+  FDSP_TRY(h->eng.apply(static_cast<const float2*>(h->in.p), n_in, &o, nullptr, &cnt, s));
+  if (cnt) FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out, o, cnt * sizeof(float2), cudaMemcpyDeviceToHost, s)));
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+/* ---------------- frequency shift ---------------- */
+int fdsp_freq_shift_create(uint32_t fs, const int32_t* shifts, uint32_t nch, fdsp_freq_shift** out) {
+  if (!out) return FDSP_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (fs == 0 || nch == 0 || !shifts) return FDSP_ERR_INVALID_ARG;
+  if (nch > (uint32_t)kMaxChannels) return FDSP_ERR_UNSUPPORTED;
+  fdsp_freq_shift* h = new (std::nothrow) fdsp_freq_shift();
+  if (!h) return FDSP_ERR_ALLOC;
+  h->fs = fs;
+  h->nco.resize(nch);
+  for (uint32_t c = 0; c < nch; ++c) h->nco[c] = make_nco(fs, shifts[c]);
+  cudaError_t e = cudaMalloc(&h->d_nco, nch * sizeof(NcoConst));
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_nco, h->nco.data(), nch * sizeof(NcoConst), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_status(e);
+  }
+  h->out.resize(nch);
+  *out = h;
+  return FDSP_OK;
+}
+
+int fdsp_freq_shift_destroy(fdsp_freq_shift* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  delete h;
+  return FDSP_OK;
+}
+
+int fdsp_freq_shift_reset(fdsp_freq_shift* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  h->abs0 = 0;
+  return FDSP_OK;
+}
+
+int fdsp_freq_shift_num_channels(const fdsp_freq_shift* h, uint32_t* n) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!n) return FDSP_ERR_INVALID_ARG;
+  *n = (uint32_t)h->nco.size();
+  return FDSP_OK;
+}
+
+int fdsp_freq_shift_counter(const fdsp_freq_shift* h, uint32_t c, uint64_t* counter) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!counter || c >= h->nco.size()) return FDSP_ERR_INVALID_ARG;
+  const uint32_t R = h->nco[c].rollover;
+  *counter = R ? h->abs0 % R : 0;
+  return FDSP_OK;
+}
+
+int fdsp_freq_shift_apply(fdsp_freq_shift* h, const fdsp_cf32* d_in, uint64_t n_in, fdsp_cf32* const* d_out,
+                          fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (n_in == 0) return FDSP_OK;
+  if (!d_in || !d_out) return FDSP_ERR_INVALID_ARG;
+  static thread_local ShiftLaunch L;
+  std::memset(&L, 0, sizeof(L));
+  L.in = reinterpret_cast<const float2*>(d_in);
+  L.N = (int64_t)n_in;
+  L.nch = (int32_t)h->nco.size();
+  L.nco = h->d_nco;
+  for (size_t c = 0; c < h->nco.size(); ++c) {
+    if (!d_out[c]) return FDSP_ERR_INVALID_ARG;
+    L.out[c] = reinterpret_cast<float2*>(d_out[c]);
+    const uint32_t R = h->nco[c].rollover;
+    L.nco_base[c] = R ? (uint32_t)(h->abs0 % R) : 0u;
+  }
+  FDSP_TRY(launch_freq_shift(L, (cudaStream_t)stream));
+  h->abs0 += n_in;
+  return FDSP_OK;
+}
+
+int fdsp_freq_shift_apply_host(fdsp_freq_shift* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* const* h_out,
+                               fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (n_in == 0) return FDSP_OK;
+  if (!h_in || !h_out) return FDSP_ERR_INVALID_ARG;
+  const size_t nch = h->nco.size();
+  cudaStream_t s = (cudaStream_t)stream;
+  FDSP_TRY(h->in.ensure(n_in * sizeof(float2) + 16));
+  std::vector<fdsp_cf32*> d(nch);
+  for (size_t c = 0; c < nch; ++c) {
+    FDSP_TRY(h->out[c].ensure(n_in * sizeof(float2) + 16));
+    d[c] = static_cast<fdsp_cf32*>(h->out[c].p);
+  }
+  FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * sizeof(float2), cudaMemcpyHostToDevice, s)));
+  FDSP_TRY(fdsp_freq_shift_apply(h, static_cast<const fdsp_cf32*>(h->in.p), n_in, d.data(), stream));
+  for (size_t c = 0; c < nch; ++c)
+    FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out[c], d[c], n_in * sizeof(float2), cudaMemcpyDeviceToHost, s)));
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+/* ---------------- polar discriminator ---------------- */
+int fdsp_polar_create(fdsp_polar** out) {
+  if (!out) return FDSP_ERR_INVALID_ARG;
+  *out = nullptr;
+  fdsp_polar* h = new (std::nothrow) fdsp_polar();
+  if (!h) return FDSP_ERR_ALLOC;
+  cudaError_t e = cudaMalloc(&h->d_prev, sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemset(h->d_prev, 0, sizeof(float2));
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_status(e);
+  }
+  *out = h;
+  return FDSP_OK;
+}
+
+int fdsp_polar_destroy(fdsp_polar* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  delete h;
+  return FDSP_OK;
+}
+
+int fdsp_polar_reset(fdsp_polar* h) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  h->have_prev = false;
+  return FDSP_OK;
+}
+
+int fdsp_polar_out_count(const fdsp_polar* h, uint64_t n_in, uint64_t* n_out) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!n_out) return FDSP_ERR_INVALID_ARG;
+  *n_out = n_in == 0 ? 0 : (h->have_prev ? n_in : n_in - 1);
+  return FDSP_OK;
+}
+
+int fdsp_polar_apply(fdsp_polar* h, const fdsp_cf32* d_in, uint64_t n_in, float* d_out, uint64_t* n_out,
+                     fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  uint64_t cnt = 0;
+  fdsp_polar_out_count(h, n_in, &cnt);
+  if (n_out) *n_out = cnt;
+  if (n_in == 0) return FDSP_OK;
+  if (!d_in || (cnt > 0 && !d_out)) return FDSP_ERR_INVALID_ARG;
+  FDSP_TRY(launch_polar(reinterpret_cast<const float2*>(d_in), (int64_t)n_in, h->d_prev, h->have_prev ? 0 : 1, d_out,
+                        (cudaStream_t)stream));
+  h->have_prev = true;
+  return FDSP_OK;
+}
+
+int fdsp_polar_apply_host(fdsp_polar* h, const fdsp_cf32* h_in, uint64_t n_in, float* h_out, uint64_t* n_out,
+                          fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  uint64_t cnt = 0;
+  fdsp_polar_out_count(h, n_in, &cnt);
+  if (n_out) *n_out = cnt;
+  if (n_in == 0) return FDSP_OK;
+  if (!h_in || (cnt > 0 && !h_out)) return FDSP_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  FDSP_TRY(h->in.ensure(n_in * sizeof(float2) + 16));
+  FDSP_TRY(h->out.ensure(n_in * sizeof(float) + 16));
+  FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * sizeof(float2), cudaMemcpyHostToDevice, s)));
+  FDSP_TRY(fdsp_polar_apply(h, static_cast<const fdsp_cf32*>(h->in.p), n_in, static_cast<float*>(h->out.p), nullptr,
+                            stream));
+  if (cnt) FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out, h->out.p, cnt * sizeof(float), cudaMemcpyDeviceToHost, s)));
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+}  // extern "C"

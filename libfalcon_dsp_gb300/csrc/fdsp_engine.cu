@@ -1,0 +1,552 @@
+// Polyphase engine: fused per-channel NCO shift + polyphase up/down resampling
+// for any number of channels sharing one input stream (plain FP32 form).
+//
+// Reference behaviour reproduced (paths relative to the reference project):
+//   shift      src/transform/falcon_dsp_freq_shift.cc:164-192, :194-235
+//   resample   src/transform/falcon_dsp_polyphase_resampler.cc:114-162, :256-346
+//   channelize src/transform/falcon_dsp_multi_rate_channelizer.cc:146-164
+//
+// Design (GB300-first, not a translation of the Jetson kernels):
+//  * Channels are grouped by decimation factor D.  For one group, one CTA owns
+//    a tile of Qt output rows and stages the RAW input span the tile needs in
+//    shared memory exactly once, de-interleaved by D (sample s at
+//    [s mod D][s div D]) so that 32 lanes computing 32 consecutive rows read
+//    32 consecutive words: no bank conflicts, whatever D is.
+//  * The NCO is folded into the taps.  For a window starting at input s with
+//    no counter rollover inside it,
+//        sum_k h[k] x[s+k] e^{j w ((s+k) mod R)} = e^{j w (s mod R)} sum_k g[k] x[s+k]
+//    with g[k] = h[k] e^{j w k}.  All channels of a group therefore read the
+//    same unshifted samples, and each output pays one rotation by an exact
+//    integer phase (64-bit fixed point turns).  A window that straddles a
+//    rollover (the reference's phase jump) is corrected exactly by splitting
+//    its sum at the rollover.
+//  * Channels with the same (up, down) share streaming state, so their outputs
+//    sit at the same input positions.  They are packed NB at a time into tap
+//    batches: one shared-memory load of x feeds NB complex MACs, which keeps
+//    the kernel FMA-bound instead of shared-memory bound.
+//  * All per-launch parameters ride in the kernel parameter block; the launch
+//    needs no host->device copy and is safe to capture in a CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+
+#include "fdsp_internal.h"
+
+namespace fdsp {
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+// e^{j 2 pi t} for a phase t given in 2^-64 turns.
+__device__ __forceinline__ float2 phasor64(uint64_t turns64) {
+  const int32_t top = (int32_t)(turns64 >> 32);
+  const float x = (float)top * 4.656612873077392578125e-10f;  // 2^-31: x in [-1, 1)
+  float s, c;
+  sincospif(x, &s, &c);
+  return make_float2(c, s);
+}
+
+template <int NB>
+__device__ __forceinline__ void load_taps(const float2* __restrict__ p, float2 (&g)[NB]) {
+  if constexpr (NB == 1) {
+    g[0] = __ldg(p);
+  } else {
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int i = 0; i < NB / 2; ++i) {
+      const float4 v = __ldg(q + i);
+      g[2 * i] = make_float2(v.x, v.y);
+      g[2 * i + 1] = make_float2(v.z, v.w);
+    }
+  }
+}
+
+// One CTA = one (decimation group, tile of Qt output rows).
+template <int NB>
+__global__ void __launch_bounds__(kThreads) poly_fp32_kernel(const __grid_constant__ PolyLaunch<NB> L) {
+  extern __shared__ float2 xs[];
+  const int g = blockIdx.x % L.ngroups;
+  const int tile = blockIdx.x / L.ngroups;
+  const GroupDesc& G = L.groups[g];
+  if (tile >= G.ntiles) return;
+  const int D = G.D, Qt = G.Qt, P = G.P;
+  const int64_t row0 = (int64_t)tile * Qt;
+  const int64_t sb = row0 * D + G.delta_min - G.tmax + 1;  // first staged input (block relative)
+  const int len = Qt * D + G.delta_span + G.tmax - 1;
+
+  // Stage the raw input span, de-interleaved by D.  Negative indices come from
+  // the history (the H samples before the block); past the block end is zero.
+  for (int t = threadIdx.x; t < len; t += blockDim.x) {
+    const int64_t v = sb + t;
+    float2 val = make_float2(0.f, 0.f);
+    if (v < 0) {
+      const int64_t hv = v + L.H;
+      if (hv >= 0) val = L.hist[hv];
+    } else if (v < L.N) {
+      val = L.block[v];
+    }
+    const int q = t / D;
+    xs[(t - q * D) * P + q] = val;
+  }
+  __syncthreads();
+
+  const int nitems = (G.ws_end - G.ws_begin) * Qt;
+  for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+    const int wq = it / Qt;
+    const int jl = it - wq * Qt;
+    const WorkSet<NB>& W = L.ws[G.ws_begin + wq];
+    const int64_t j = row0 + jl;
+    if (j >= W.J) continue;
+    const int T = W.T;
+    const int a0 = (W.delta - G.delta_min) + (G.tmax - T);
+    int bq = a0 / D;
+    int b = a0 - bq * D;
+    int q = bq + jl;
+
+    float2 acc[NB];
+#pragma unroll
+    for (int n = 0; n < NB; ++n) acc[n] = make_float2(0.f, 0.f);
+
+    const float2* __restrict__ tp = W.taps;
+    for (int k = 0; k < T; ++k) {
+      const float2 x = xs[b * P + q];
+      float2 gk[NB];
+      load_taps<NB>(tp + (size_t)k * NB, gk);
+#pragma unroll
+      for (int n = 0; n < NB; ++n) {
+        acc[n].x = fmaf(gk[n].x, x.x, acc[n].x);
+        acc[n].x = fmaf(-gk[n].y, x.y, acc[n].x);
+        acc[n].y = fmaf(gk[n].x, x.y, acc[n].y);
+        acc[n].y = fmaf(gk[n].y, x.x, acc[n].y);
+      }
+      if (++b == D) {
+        b = 0;
+        ++q;
+      }
+    }
+
+    // Epilogue: rotate by the NCO phase of the window start, fix rollover
+    // straddles, store.
+    const int64_t m = (int64_t)W.r + (int64_t)W.U * j;
+    const int64_t w = (int64_t)W.delta + j * D - T + 1;  // window start, block relative
+#pragma unroll
+    for (int n = 0; n < NB; ++n) {
+      if (n >= W.nb) break;
+      const int c = W.ch[n];
+      float2 y = acc[n];
+      const NcoConst nc = L.nco[c];
+      if (nc.enabled) {
+        const uint32_t R = nc.rollover;
+        const int64_t pv = (int64_t)L.nco_base[c] + w;
+        uint64_t p;
+        if (pv < 0) {
+          p = (uint64_t)(pv + (int64_t)R);
+        } else if (pv < 0x100000000LL) {
+          p = (uint32_t)pv % R;
+        } else {
+          p = (uint64_t)pv % R;
+        }
+        const uint64_t ph = p * nc.omega64;
+        const float2 e = phasor64(ph);
+        if (p + (uint64_t)T - 1 >= (uint64_t)R) {
+          // The window crosses the counter rollover: samples from k0 on use
+          // angle w*(p + k - R) instead of w*(p + k).
+          const int k0 = (int)((uint64_t)R - p);
+          float2 B = make_float2(0.f, 0.f);
+          int kb = a0 + k0;
+          int qq = kb / D;
+          int bb = kb - qq * D;
+          qq += jl;
+          for (int k = k0; k < T; ++k) {
+            const float2 x = xs[bb * P + qq];
+            const float2 gk = __ldg(tp + (size_t)k * NB + n);
+            B.x = fmaf(gk.x, x.x, B.x);
+            B.x = fmaf(-gk.y, x.y, B.x);
+            B.y = fmaf(gk.x, x.y, B.y);
+            B.y = fmaf(gk.y, x.x, B.y);
+            if (++bb == D) {
+              bb = 0;
+              ++qq;
+            }
+          }
+          const float2 e2 = phasor64(ph - nc.wrap64);
+          const float2 A = make_float2(y.x - B.x, y.y - B.y);
+          const float2 ya = cmul(A, e), yb = cmul(B, e2);
+          y = make_float2(ya.x + yb.x, ya.y + yb.y);
+        } else {
+          y = cmul(y, e);
+        }
+      }
+      L.out[c][m] = y;
+    }
+  }
+}
+
+// History after a block: the last H samples of [old history | block].
+__global__ void hist_update_kernel(const float2* __restrict__ old_hist, const float2* __restrict__ block, int64_t N,
+                                   int H, float2* __restrict__ new_hist) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= H) return;
+  const int64_t v = N + i;
+  new_hist[i] = v < H ? old_hist[v] : block[v - H];
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+NcoConst make_nco(uint32_t fs, int32_t f) {
+  NcoConst n;
+  std::memset(&n, 0, sizeof(n));
+  if (f == 0 || fs == 0) return n;
+  // rollover index: falcon_dsp_freq_shift.cc:216-229
+  double r = (double)fs / (double)std::llabs((long long)f);
+  while (r < 1e5) r *= 10.0;
+  const uint32_t R = (uint32_t)std::round(r);
+  int64_t fm = (int64_t)f % (int64_t)fs;
+  if (fm < 0) fm += fs;
+  const unsigned __int128 num = ((unsigned __int128)(uint64_t)fm << 64) + (fs / 2);
+  const uint64_t w = (uint64_t)(num / fs);
+  n.omega64 = w;
+  n.wrap64 = (uint64_t)R * w;
+  n.rollover = R;
+  n.enabled = (R != 0) ? 1u : 0u;
+  return n;
+}
+
+PolyEngine::~PolyEngine() {
+  for (auto& b : batches_) {
+    if (b.d_taps) cudaFree(b.d_taps);
+  }
+  if (d_nco_) cudaFree(d_nco_);
+  for (auto& h : d_hist_) {
+    if (h) cudaFree(h);
+  }
+}
+
+static int choose_qt(uint32_t D, int tmax) {
+  // ~8K input samples per tile, at least one warp of rows, shared memory
+  // (tile + halo + offset spread, de-interleaved) under ~200 KB.
+  int qt = (int)((8192 / D) & ~31u);
+  if (qt < 32) qt = 32;
+  auto bytes = [&](int q) {
+    const int64_t len = (int64_t)q * D + 3LL * D + tmax;
+    const int64_t P = len / D + 2;
+    return (int64_t)D * P * 8;
+  };
+  while (qt > 32 && bytes(qt) > 200 * 1024) qt -= 32;
+  if (bytes(qt) > 200 * 1024) return -1;
+  return qt;
+}
+
+int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool complex_taps) {
+  if (nch == 0 || ch == nullptr) return FDSP_ERR_INVALID_ARG;
+  if (nch > (uint32_t)kMaxChannels) return FDSP_ERR_UNSUPPORTED;
+  fs_ = fs;
+  complex_taps_ = complex_taps;
+  chans_.resize(nch);
+  cls_of_.assign(nch, -1);
+  int tmax_all = 1;
+  for (uint32_t c = 0; c < nch; ++c) {
+    const fdsp_channel_cfg& cc = ch[c];
+    if (cc.up_rate == 0 || cc.down_rate == 0 || cc.num_coeffs == 0 || cc.resample_filter_coeffs == nullptr)
+      return FDSP_ERR_INVALID_ARG;
+    EngineChannel& e = chans_[c];
+    e.up = cc.up_rate;
+    e.down = cc.down_rate;
+    // polyphase_resampler.cc:131-157 -- pad to a multiple of up, transpose, flip
+    uint32_t padded = cc.num_coeffs;
+    while (padded % e.up) padded++;
+    e.T = padded / e.up;
+    e.flipped.assign((size_t)padded, make_float2(0.f, 0.f));
+    for (uint32_t ph = 0; ph < e.up; ++ph) {
+      for (uint32_t jj = 0; jj < e.T; ++jj) {
+        const uint64_t src = (uint64_t)jj * e.up + ph;
+        if (src < cc.num_coeffs) {
+          const fdsp_cf32 v = cc.resample_filter_coeffs[src];
+          e.flipped[(size_t)ph * e.T + (e.T - 1 - jj)] = make_float2(v.re, complex_taps ? v.im : 0.f);
+        }
+      }
+    }
+    e.shift_hz = (int32_t)cc.freq_shift_in_hz;  // initialize(uint32_t, int32_t) truncation
+    e.nco = make_nco(fs, e.shift_hz);
+    if (e.nco.enabled && e.T > e.nco.rollover) return FDSP_ERR_UNSUPPORTED;
+    tmax_all = std::max(tmax_all, (int)e.T);
+    // class by (up, down)
+    int k = -1;
+    for (size_t i = 0; i < classes_.size(); ++i) {
+      if (classes_[i].up == e.up && classes_[i].down == e.down) k = (int)i;
+    }
+    if (k < 0) {
+      EngineClass nc;
+      nc.up = e.up;
+      nc.down = e.down;
+      nc.phase = 0;
+      nc.xoffset = 0;
+      nc.M = 0;
+      classes_.push_back(nc);
+      k = (int)classes_.size() - 1;
+    }
+    classes_[k].chans.push_back((int)c);
+    cls_of_[c] = k;
+  }
+  H_ = tmax_all - 1;
+
+  // NB: channels per tap batch (largest class decides, power of two <= 8)
+  size_t maxcls = 1;
+  for (auto& k : classes_) maxcls = std::max(maxcls, k.chans.size());
+  nb_ = maxcls >= 8 ? 8 : maxcls >= 4 ? 4 : maxcls >= 2 ? 2 : 1;
+
+  // decimation groups
+  std::map<uint32_t, int> gidx;
+  for (auto& k : classes_) {
+    if (!gidx.count(k.down)) {
+      gidx[k.down] = (int)groups_.size();
+      EngineGroup g;
+      g.D = k.down;
+      g.Qt = 0;
+      groups_.push_back(g);
+    }
+  }
+  if (groups_.size() > (size_t)kMaxGroups) return FDSP_ERR_UNSUPPORTED;
+
+  // batches: within a class, channels sorted by taps per phase (descending)
+  for (size_t ki = 0; ki < classes_.size(); ++ki) {
+    std::vector<int> cs = classes_[ki].chans;
+    std::stable_sort(cs.begin(), cs.end(), [&](int a, int b) { return chans_[a].T > chans_[b].T; });
+    for (size_t i = 0; i < cs.size(); i += nb_) {
+      EngineBatch bt;
+      bt.cls = (int)ki;
+      bt.group = gidx[classes_[ki].down];
+      bt.chans.assign(cs.begin() + i, cs.begin() + std::min(cs.size(), i + nb_));
+      bt.T = (int)chans_[bt.chans[0]].T;
+      bt.d_taps = nullptr;
+      groups_[bt.group].batches.push_back((int)batches_.size());
+      batches_.push_back(bt);
+    }
+  }
+  for (auto& g : groups_) {
+    int tmax = 1;
+    for (int b : g.batches) tmax = std::max(tmax, batches_[b].T);
+    g.Qt = choose_qt(g.D, tmax);
+    if (g.Qt < 0) return FDSP_ERR_UNSUPPORTED;
+  }
+
+  // modulated, padded taps of every batch: [up][T][NB]
+  for (auto& bt : batches_) {
+    const uint32_t U = classes_[bt.cls].up;
+    std::vector<float2> host((size_t)U * bt.T * nb_, make_float2(0.f, 0.f));
+    for (size_t n = 0; n < bt.chans.size(); ++n) {
+      const EngineChannel& e = chans_[bt.chans[n]];
+      const int pad = bt.T - (int)e.T;
+      int64_t fm = 0;
+      if (e.nco.enabled) {
+        fm = (int64_t)e.shift_hz % (int64_t)fs;
+        if (fm < 0) fm += fs;
+      }
+      for (uint32_t ph = 0; ph < U; ++ph) {
+        for (int k = pad; k < bt.T; ++k) {
+          const float2 h = e.flipped[(size_t)ph * e.T + (k - pad)];
+          double gr = h.x, gi = h.y;
+          if (e.nco.enabled) {
+            // e^{j w k} with w k reduced exactly: 2 pi ((f mod fs) k mod fs) / fs
+            const uint64_t red = (uint64_t)(((unsigned __int128)(uint64_t)fm * (uint64_t)k) % fs);
+            const double ang = 2.0 * M_PI * (double)red / (double)fs;
+            const double c = std::cos(ang), s = std::sin(ang);
+            gr = (double)h.x * c - (double)h.y * s;
+            gi = (double)h.x * s + (double)h.y * c;
+          }
+          host[((size_t)ph * bt.T + k) * nb_ + n] = make_float2((float)gr, (float)gi);
+        }
+      }
+    }
+    cudaError_t e = cudaMalloc(&bt.d_taps, host.size() * sizeof(float2));
+    if (e != cudaSuccess) return cuda_status(e);
+    e = cudaMemcpy(bt.d_taps, host.data(), host.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+
+  std::vector<NcoConst> nco(nch);
+  for (uint32_t c = 0; c < nch; ++c) nco[c] = chans_[c].nco;
+  cudaError_t e = cudaMalloc(&d_nco_, nch * sizeof(NcoConst));
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaMemcpy(d_nco_, nco.data(), nch * sizeof(NcoConst), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (H_ > 0) {
+    for (auto& h : d_hist_) {
+      e = cudaMalloc(&h, (size_t)H_ * sizeof(float2));
+      if (e != cudaSuccess) return cuda_status(e);
+      e = cudaMemset(h, 0, (size_t)H_ * sizeof(float2));
+      if (e != cudaSuccess) return cuda_status(e);
+    }
+  }
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_status(e);
+  return FDSP_OK;
+}
+
+// Outputs the reference loop emits for n inputs from (phase, xoffset):
+// the m >= 0 with xoffset + floor((phase + m*down)/up) < n.
+uint64_t polyphase_out_count(uint32_t up, uint32_t down, uint32_t phase, uint64_t xoffset, uint64_t n) {
+  if (xoffset >= n) return 0;
+  const unsigned __int128 lim = (unsigned __int128)up * (n - xoffset);  // > phase
+  return (uint64_t)((lim - phase + down - 1) / down);
+}
+
+// State after M outputs of an apply of n inputs (polyphase_resampler.cc:303-312).
+void polyphase_advance(uint32_t up, uint32_t down, uint32_t& phase, uint64_t& xoffset, uint64_t n, uint64_t M) {
+  if (xoffset >= n) {
+    xoffset -= n;
+    return;
+  }
+  const unsigned __int128 t = (unsigned __int128)phase + (unsigned __int128)M * down;
+  const uint64_t x_new = xoffset + (uint64_t)(t / up);
+  phase = (uint32_t)(t % up);
+  xoffset = x_new - n;
+}
+
+static uint64_t class_out_count(const EngineClass& k, uint64_t n) {
+  return polyphase_out_count(k.up, k.down, k.phase, k.xoffset, n);
+}
+
+int PolyEngine::out_counts(uint64_t n_in, uint64_t* n_out) const {
+  if (!n_out) return FDSP_ERR_INVALID_ARG;
+  for (size_t c = 0; c < chans_.size(); ++c) n_out[c] = class_out_count(classes_[cls_of_[c]], n_in);
+  return FDSP_OK;
+}
+
+void PolyEngine::reset() {
+  for (auto& k : classes_) {
+    k.phase = 0;
+    k.xoffset = 0;
+  }
+  abs0_ = 0;
+  cudaDeviceSynchronize();
+  for (auto& h : d_hist_) {
+    if (h) cudaMemset(h, 0, (size_t)H_ * sizeof(float2));
+  }
+  hist_cur_ = 0;
+  cudaDeviceSynchronize();
+}
+
+template <int NB>
+int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream) {
+  static thread_local PolyLaunch<NB> L;  // ~20 KB: keep it off the stack
+  std::memset(&L, 0, sizeof(L));
+  L.block = d_in;
+  L.hist = d_hist_[hist_cur_];
+  L.N = (int64_t)n;
+  L.H = H_;
+  L.nco = d_nco_;
+  for (size_t c = 0; c < chans_.size(); ++c) {
+    L.out[c] = out[c];
+    const uint32_t R = chans_[c].nco.rollover;
+    L.nco_base[c] = R ? (uint32_t)(abs0_ % R) : 0u;
+  }
+  int ng = 0, nws = 0, max_tiles = 0;
+  size_t smem_max = 0;
+  for (auto& g : groups_) {
+    GroupDesc& gd = L.groups[ng];
+    gd.D = (int32_t)g.D;
+    gd.Qt = g.Qt;
+    gd.ws_begin = nws;
+    int dmin = INT32_MAX, dmax = INT32_MIN, tmax = 1;
+    int64_t rows = 0;
+    for (int bi : g.batches) {
+      const EngineBatch& bt = batches_[bi];
+      const EngineClass& k = classes_[bt.cls];
+      const uint32_t U = k.up;
+      for (uint32_t r = 0; r < U; ++r) {
+        if (k.M <= r) continue;
+        const uint64_t J = (k.M - r + U - 1) / U;
+        const uint64_t t = (uint64_t)k.phase + (uint64_t)r * g.D;
+        const uint64_t delta = k.xoffset + t / U;
+        const uint32_t phi = (uint32_t)(t % U);
+        if (nws >= kMaxWorkSets) return FDSP_ERR_UNSUPPORTED;
+        WorkSet<NB>& W = L.ws[nws++];
+        W.taps = bt.d_taps + (size_t)phi * bt.T * NB;
+        W.T = bt.T;
+        W.delta = (int32_t)delta;
+        W.J = (int32_t)J;
+        W.U = (int32_t)U;
+        W.r = (int32_t)r;
+        W.nb = (int32_t)bt.chans.size();
+        for (size_t i = 0; i < bt.chans.size(); ++i) W.ch[i] = (int16_t)bt.chans[i];
+        dmin = std::min(dmin, (int)delta);
+        dmax = std::max(dmax, (int)delta);
+        tmax = std::max(tmax, bt.T);
+        rows = std::max<int64_t>(rows, (int64_t)J);
+      }
+    }
+    gd.ws_end = nws;
+    if (gd.ws_end == gd.ws_begin) continue;
+    gd.tmax = tmax;
+    gd.delta_min = dmin;
+    gd.delta_span = dmax - dmin;
+    gd.ntiles = (int32_t)((rows + g.Qt - 1) / g.Qt);
+    const int64_t len = (int64_t)g.Qt * g.D + gd.delta_span + tmax - 1;
+    int64_t P = (len + g.D - 1) / g.D;
+    if ((P & 1) == 0) P++;  // odd pitch: the staging scatter spreads over banks
+    gd.P = (int32_t)P;
+    smem_max = std::max(smem_max, (size_t)(g.D * P * sizeof(float2)));
+    max_tiles = std::max(max_tiles, gd.ntiles);
+    ng++;
+  }
+  L.ngroups = ng;
+  L.max_tiles = max_tiles;
+  L.nws = nws;
+  launches_last_ = 0;
+  if (ng > 0 && max_tiles > 0) {
+    if (smem_max > 227 * 1024) return FDSP_ERR_UNSUPPORTED;
+    cudaError_t e = cudaFuncSetAttribute(poly_fp32_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem_max);
+    if (e != cudaSuccess) return cuda_status(e);
+    const int64_t nblocks = (int64_t)ng * max_tiles;
+    if (nblocks > 0x7fffffffLL) return FDSP_ERR_UNSUPPORTED;
+    poly_fp32_kernel<NB><<<(unsigned)nblocks, kThreads, smem_max, stream>>>(L);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+    launches_last_++;
+  }
+  if (H_ > 0) {
+    hist_update_kernel<<<(H_ + 255) / 256, 256, 0, stream>>>(d_hist_[hist_cur_], d_in, (int64_t)n, H_,
+                                                              d_hist_[hist_cur_ ^ 1]);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+    hist_cur_ ^= 1;
+    launches_last_++;
+  }
+  return FDSP_OK;
+}
+
+int PolyEngine::apply(const float2* d_in, uint64_t n, float2* const* out, const uint64_t* cap, uint64_t* n_out,
+                      cudaStream_t stream) {
+  if (n > 0 && d_in == nullptr) return FDSP_ERR_INVALID_ARG;
+  if (n >= (1ull << 31)) return FDSP_ERR_UNSUPPORTED;
+  for (auto& k : classes_) k.M = class_out_count(k, n);
+  for (size_t c = 0; c < chans_.size(); ++c) {
+    const uint64_t M = classes_[cls_of_[c]].M;
+    if (n_out) n_out[c] = M;
+    if (M > 0 && (out == nullptr || out[c] == nullptr)) return FDSP_ERR_INVALID_ARG;
+    if (cap && cap[c] < M) return FDSP_ERR_CAPACITY;
+  }
+  if (n == 0) return FDSP_OK;
+  int st;
+  switch (nb_) {
+    case 1: st = launch<1>(d_in, n, out, stream); break;
+    case 2: st = launch<2>(d_in, n, out, stream); break;
+    case 4: st = launch<4>(d_in, n, out, stream); break;
+    default: st = launch<8>(d_in, n, out, stream); break;
+  }
+  if (st != FDSP_OK) return st;
+  // advance the streaming state (polyphase_resampler.cc:303-312)
+  for (auto& k : classes_) polyphase_advance(k.up, k.down, k.phase, k.xoffset, n, k.M);
+  abs0_ += n;
+  return FDSP_OK;
+}
+
+}  // namespace fdsp

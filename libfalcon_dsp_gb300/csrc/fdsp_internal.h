@@ -1,0 +1,174 @@
+// Internal declarations shared by the CUDA translation units of
+// libfalcon_dsp_gb300.  Nothing here is part of the public C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "fdsp_c.h"
+
+namespace fdsp {
+
+// ---------------------------------------------------------------------------
+// Limits of one polyphase-engine launch.  Every field of the launch travels in
+// the kernel parameter block (CUDA allows up to 32 764 bytes on sm_70+), so a
+// launch needs no host->device copy and can be captured into a CUDA graph.
+// ---------------------------------------------------------------------------
+constexpr int kMaxChannels = 512;   // output channels per engine
+constexpr int kMaxGroups = 16;      // distinct decimation factors per engine
+constexpr int kMaxWorkSets = 256;   // (tap batch, output class) pairs per launch
+constexpr int kThreads = 256;       // threads per CTA of the FP32 engine kernel
+
+// Per-channel NCO constants (device array, written once at create time).
+// The reference's angle for input sample n of a channel is
+//   omega * (n mod R),  omega = 2*pi*f/fs          (falcon_dsp_freq_shift.cc:164-192)
+// Here the angle is carried as a 64-bit fixed-point fraction of a turn:
+//   turns(p) = p * omega64 mod 2^64, omega64 = round(2^64 * (f mod fs) / fs)
+// which is exact to ~1e-9 rad for every p < R.
+struct NcoConst {
+  uint64_t omega64;   // turns per sample, 2^-64 units
+  uint64_t wrap64;    // R * omega64 mod 2^64 (phase that the rollover drops)
+  uint32_t rollover;  // R; 0 when the channel has no shift
+  uint32_t enabled;   // 0: phasor is exactly 1 (shift of 0 Hz)
+};
+
+// One decimation-factor group of an engine launch (one CTA per tile of it).
+struct GroupDesc {
+  int32_t D;          // down rate shared by every channel of the group
+  int32_t Qt;         // output rows per tile (multiple of 32)
+  int32_t P;          // shared-memory pitch (float2) of the de-interleaved tile
+  int32_t tmax;       // longest padded window (taps) of the group
+  int32_t delta_min;  // smallest window-end offset of any active output class
+  int32_t delta_span; // delta_max - delta_min
+  int32_t ntiles;     // tiles of Qt rows in this launch
+  int32_t ws_begin;   // work sets [ws_begin, ws_end) belong to this group
+  int32_t ws_end;
+  int32_t pad_;
+};
+
+// One (tap batch, output class r) pair of a launch.  Output j of the class is
+// output index m = r + U*j of every channel in the batch; its window is
+// [delta + j*D - T + 1, delta + j*D] in block-relative input indices.
+template <int NB>
+struct WorkSet {
+  const float2* taps;   // [T][NB] modulated taps of phase phi_r
+  int32_t T;            // padded taps per phase of the batch
+  int32_t delta;        // window end of row j = 0 (block relative)
+  int32_t J;            // rows that have an output in this launch
+  int32_t U;            // up rate of the batch's channels
+  int32_t r;            // output class (m mod U)
+  int32_t nb;           // live channels in the batch (<= NB)
+  int16_t ch[NB];       // channel ids
+};
+
+template <int NB>
+struct PolyLaunch {
+  const float2* block;      // device input block (N samples)
+  const float2* hist;       // device history (H samples preceding block)
+  int64_t N;
+  int32_t H;
+  int32_t ngroups;
+  int32_t max_tiles;
+  int32_t nws;
+  const NcoConst* nco;      // [nch]
+  GroupDesc groups[kMaxGroups];
+  WorkSet<NB> ws[kMaxWorkSets];
+  float2* out[kMaxChannels];         // output base of each channel for this launch
+  uint32_t nco_base[kMaxChannels];   // (samples since reset at block[0]) mod R
+};
+
+// CUDA error -> status, remembering the CUDA code for fdsp_last_cuda_error().
+int cuda_status(cudaError_t e);
+void set_last_cuda_error(int code);
+
+// ---------------------------------------------------------------------------
+// Polyphase engine: the shared machinery behind the channelizer, the
+// standalone resampler and the FIR filter.
+// ---------------------------------------------------------------------------
+struct EngineChannel {
+  uint32_t up, down;
+  uint32_t T;                  // taps per phase (reference coeffs_per_phase)
+  int32_t shift_hz;            // int32 shift, as the reference's NCO stores it
+  std::vector<float2> flipped; // [up][T] transposed & flipped taps
+  NcoConst nco;
+};
+
+struct EngineClass {   // channels with identical (up, down) share streaming state
+  uint32_t up, down;
+  uint32_t phase;      // reference coeff_phase
+  uint64_t xoffset;    // reference xOffset
+  uint64_t M;          // outputs of the current launch
+  std::vector<int> chans;
+};
+
+struct EngineBatch {
+  int cls;             // class index
+  int group;           // decimation group index
+  int T;               // padded taps per phase
+  std::vector<int> chans;
+  float2* d_taps;      // [up][T][NB] on the device
+};
+
+struct EngineGroup {
+  uint32_t D;
+  int Qt;
+  std::vector<int> batches;
+};
+
+class PolyEngine {
+ public:
+  // complex_taps: FIR semantics (taps used as complex numbers);
+  // otherwise resampler semantics (only the real part of each tap is used,
+  // falcon_dsp_polyphase_resampler.cc:286-299).
+  int init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool complex_taps);
+  ~PolyEngine();
+
+  int out_counts(uint64_t n_in, uint64_t* n_out) const;
+  // Enqueue one streaming block on `stream`; outputs of channel c go to out[c]
+  // (device pointers, capacity checked against cap[c] when cap != nullptr).
+  int apply(const float2* d_in, uint64_t n, float2* const* out, const uint64_t* cap, uint64_t* n_out,
+            cudaStream_t stream);
+  void reset();
+
+  uint32_t num_channels() const { return (uint32_t)chans_.size(); }
+  uint32_t coeffs_per_phase(int c) const { return chans_[c].T; }
+  uint32_t phase_of(int c) const { return classes_[cls_of_[c]].phase; }
+  uint64_t xoffset_of(int c) const { return classes_[cls_of_[c]].xoffset; }
+  uint64_t samples_since_reset() const { return abs0_; }
+  int history_len() const { return H_; }
+  int nb() const { return nb_; }
+  // Test/diagnostic hook: force the FP32 kernel's NB template (1,2,4,8).
+  int kernel_launches_last() const { return launches_last_; }
+
+ private:
+  template <int NB>
+  int launch(const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream);
+
+  uint32_t fs_ = 0;
+  bool complex_taps_ = false;
+  int nb_ = 1;
+  int H_ = 0;                       // history length (max T - 1)
+  std::vector<EngineChannel> chans_;
+  std::vector<EngineClass> classes_;
+  std::vector<int> cls_of_;
+  std::vector<EngineBatch> batches_;
+  std::vector<EngineGroup> groups_;
+  NcoConst* d_nco_ = nullptr;
+  float2* d_hist_[2] = {nullptr, nullptr};
+  int hist_cur_ = 0;
+  uint64_t abs0_ = 0;               // samples since reset at the next block
+  int launches_last_ = 0;
+};
+
+// NCO constants of a (fs, f) pair, following falcon_dsp_freq_shift.cc:194-235.
+NcoConst make_nco(uint32_t fs, int32_t f);
+
+// Closed-form index bookkeeping of the reference's resampler loop.
+uint64_t polyphase_out_count(uint32_t up, uint32_t down, uint32_t phase, uint64_t xoffset, uint64_t n);
+void polyphase_advance(uint32_t up, uint32_t down, uint32_t& phase, uint64_t& xoffset, uint64_t n, uint64_t M);
+
+static_assert(sizeof(PolyLaunch<8>) <= 32764, "engine launch must fit the kernel parameter block");
+
+}  // namespace fdsp

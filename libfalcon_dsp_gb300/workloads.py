@@ -1,0 +1,145 @@
+"""Seeded synthetic workloads of the channelizer benchmarks.
+
+No public dataset is involved: every input is generated from a seed with the
+shapes, rates and value distributions of the benchmark configurations.
+
+* ``channelizer_256``  2^26 complex<float> samples at 61.44 MSps (512 random
+  tones, amplitudes U[0.1, 1], random phases, plus CN(0, 0.01^2) noise); 256
+  output channels with decimation D in {8,16,25,40,64,125,160,320}, up-factor
+  U in {1,2,3} and 12-64 taps per phase (Kaiser-windowed sinc, beta 8.6); each
+  channel's NCO brings one tone to DC.
+* ``resampler_1ch``    2^20 samples at 48 kHz (3 tones + noise), 147/160,
+  Kaiser sinc beta 8.6 with 3528 taps (24 per phase).
+* ``channelizer_8ch``  2^24 samples at 10 MSps (tones stand in for the QPSK
+  carriers of the spec at the same centre-frequency spread), 8 channels with
+  ratios 1/40, 3/125, 1/80, 2/625, 1/50, 1/20, 3/200, 1/100, 16-48 taps per
+  phase, streamed in 2^16-sample blocks.
+
+Tones sit on the frequency grid of the signal length so a whole signal is one
+inverse FFT of a sparse spectrum (fast at 2^26 samples).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+from scipy import signal as _sig
+
+C3_DECIM = [8, 16, 25, 40, 64, 125, 160, 320]
+C3_UP = [1, 2, 3]
+
+
+def kaiser_lowpass(up: int, down: int, taps_per_phase: int, beta: float = 8.6) -> np.ndarray:
+    """Anti-alias lowpass for an up/down resampler: U*T taps at the upsampled
+    rate, cutoff at the narrower of the two Nyquist bands, passband gain U."""
+    n = up * taps_per_phase
+    h = _sig.firwin(n, 1.0 / max(up, down), window=("kaiser", beta))
+    return (up * h).astype(np.complex64)
+
+
+def _tones(rng, n, fs, tones, max_freq):
+    lim = fs / 2 if max_freq is None else max_freq
+    bins = rng.integers(-int(lim / fs * n), int(lim / fs * n), size=tones)
+    amp = rng.uniform(0.1, 1.0, size=tones)
+    ph = rng.uniform(0, 2 * np.pi, size=tones)
+    return bins, amp, ph, bins * fs / n
+
+
+def tone_freqs(n: int, fs: float, tones: int, seed: int, max_freq: float | None = None) -> np.ndarray:
+    """Tone frequencies tone_signal(n, fs, tones, seed) would use, without
+    synthesising the signal."""
+    return _tones(np.random.default_rng(seed), n, fs, tones, max_freq)[3]
+
+
+def tone_signal(n: int, fs: float, tones: int, seed: int, noise_sigma: float = 0.01, max_freq: float | None = None,
+                device=None):
+    """Sum of `tones` complex tones + complex Gaussian noise.  Returns
+    (samples complex64, tone frequencies in Hz).  With `device` (a torch CUDA
+    device) the signal is synthesised on the GPU and returned as a tensor."""
+    rng = np.random.default_rng(seed)
+    bins, amp, ph, freqs = _tones(rng, n, fs, tones, max_freq)
+    if device is None:
+        spec = np.zeros(n, np.complex128)
+        np.add.at(spec, bins % n, amp * np.exp(1j * ph))
+        x = np.fft.ifft(spec) * n
+        x += (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * (noise_sigma / math.sqrt(2))
+        return x.astype(np.complex64), freqs
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    spec = torch.zeros(n, dtype=torch.complex64, device=device)
+    vals = torch.tensor(amp * np.exp(1j * ph), dtype=torch.complex64, device=device)
+    spec.index_add_(0, torch.tensor(bins % n, device=device), vals)
+    x = torch.fft.ifft(spec) * n
+    noise = torch.randn(n, dtype=torch.complex64, device=device, generator=g) * noise_sigma
+    return (x + noise).contiguous(), freqs
+
+
+def channelizer_256_plan(fs: float = 61.44e6, tone_freqs=None, nch: int = 256, seed: int = 3) -> list[dict]:
+    rng = np.random.default_rng(seed)
+    chans = []
+    for c in range(nch):
+        d = int(rng.choice(C3_DECIM))
+        u = int(rng.choice(C3_UP))
+        g = math.gcd(u, d)
+        u, d = u // g, d // g
+        t = int(rng.integers(12, 65))
+        if tone_freqs is not None and len(tone_freqs):
+            f = -int(round(float(tone_freqs[int(rng.integers(0, len(tone_freqs)))])))
+        else:
+            f = int(rng.integers(-int(fs / 2), int(fs / 2)))
+        chans.append(dict(output_sample_rate_in_sps=int(fs * u / d), freq_shift_in_hz=f, up_rate=u, down_rate=d,
+                          coeffs=kaiser_lowpass(u, d, t)))
+    return chans
+
+
+def channelizer_256(n: int = 1 << 26, seed: int = 2026, device=None):
+    fs = 61.44e6
+    x, freqs = tone_signal(n, fs, 512, seed, device=device)
+    return x, int(fs), channelizer_256_plan(fs, freqs, 256, seed + 1)
+
+
+def channelizer_256_cpu_sample(n_sample: int, n: int = 1 << 26, seed: int = 2026):
+    """A bounded CPU sample of channelizer_256: the same 256-channel plan (NCOs
+    from the full-length signal's tones) over an n_sample-sample signal drawn
+    from the same distribution."""
+    fs = 61.44e6
+    chans = channelizer_256_plan(fs, tone_freqs(n, fs, 512, seed), 256, seed + 1)
+    x, _ = tone_signal(n_sample, fs, 512, seed)
+    return x, int(fs), chans
+
+
+def resampler_1ch(n: int = 1 << 20, seed: int = 2024, device=None):
+    fs = 48000.0
+    x, _ = tone_signal(n, fs, 3, seed, max_freq=20000.0, device=device)
+    return x, 147, 160, kaiser_lowpass(147, 160, 24)
+
+
+C2_RATIOS = [(1, 40), (3, 125), (1, 80), (2, 625), (1, 50), (1, 20), (3, 200), (1, 100)]
+
+
+def channelizer_8ch(n: int = 1 << 24, seed: int = 2025, device=None):
+    fs = 10e6
+    x, freqs = tone_signal(n, fs, 16, seed, max_freq=4.5e6, device=device)
+    rng = np.random.default_rng(seed + 1)
+    chans = []
+    for c, (u, d) in enumerate(C2_RATIOS):
+        t = int(rng.integers(16, 49))
+        chans.append(dict(output_sample_rate_in_sps=int(fs * u / d), freq_shift_in_hz=-int(round(freqs[c])),
+                          up_rate=u, down_rate=d, coeffs=kaiser_lowpass(u, d, t)))
+    return x, int(fs), chans
+
+
+def algorithmic_bytes(n_in: int, n_out_total: int) -> int:
+    """HBM bytes one apply must move: the complex64 input read once plus every
+    complex64 output written once (taps, history and NCO state excluded)."""
+    return 8 * n_in + 8 * n_out_total
+
+
+def algorithmic_flops(chans: list[dict], n_out: list[int]) -> int:
+    """4 flops per real tap x complex sample, T taps per phase per output."""
+    tot = 0
+    for ch, m in zip(chans, n_out):
+        t = -(-len(ch["coeffs"]) // ch["up_rate"])
+        tot += 4 * t * m
+    return tot
