@@ -234,6 +234,9 @@ def run_ours(args) -> None:
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    nl = C.c_uint32()
+    lib.fdsp_channelizer_kernel_launches(ch._h, C.byref(nl))
+    launches_per_step = nl.value
 
     gpu_id = None
     try:
@@ -330,7 +333,7 @@ def run_ours(args) -> None:
             "config": {"workload": WORKLOAD, "n_in": x.numel(), "channels": nch, "seed": SEED, "path": "plain FP32",
                        "l2": "no flush: each step reads 512 MiB and writes ~9.6 GB, far above the 129 MB L2",
                        "parallelism": f"replicas x{world}"},
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": launches_per_step * args.steps,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         }
         print(json.dumps(line), flush=True)

@@ -116,6 +116,8 @@ int fdsp_channelizer_out_count(const fdsp_channelizer *h, uint64_t n_in, uint64_
  * NULL to skip the check) receives n_out[c] samples. */
 int fdsp_channelizer_apply(fdsp_channelizer *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *const *d_out,
                            const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);
+/* Kernel launches the most recent apply enqueued (diagnostics, profiling). */
+int fdsp_channelizer_kernel_launches(const fdsp_channelizer *h, uint32_t *n);
 /* apply(in, out) on host buffers (copies in, computes, copies out, syncs). */
 int fdsp_channelizer_apply_host(fdsp_channelizer *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,
                                 const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);

@@ -69,6 +69,7 @@ SIGNATURES = {
     "fdsp_channelizer_out_count": [_vp, _u64, _pu64],
     "fdsp_channelizer_apply": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
     "fdsp_channelizer_apply_host": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
+    "fdsp_channelizer_kernel_launches": [_vp, _pu32],
     "fdsp_resampler_create": [_u32, _u32, _vp, _u32, _pp],
     "fdsp_resampler_destroy": [_vp],
     "fdsp_resampler_reset": [_vp],

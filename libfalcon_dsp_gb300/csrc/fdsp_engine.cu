@@ -42,147 +42,240 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
-// e^{j 2 pi t} for a phase t given in 2^-64 turns.
-__device__ __forceinline__ float2 phasor64(uint64_t turns64) {
+// (pv mod R) for 0 <= pv < 2^32 with a precomputed M = ceil(2^64 / R)
+// (Lemire, Kaser & Kurz, "Faster remainder by direct computation", 2019).
+__device__ __forceinline__ uint32_t fastmod_u32(uint32_t a, uint64_t M, uint32_t R) {
+  return (uint32_t)__umul64hi(M * (uint64_t)a, (uint64_t)R);
+}
+
+// Counter value (n mod R) of the sample at block-relative index w.
+__device__ __forceinline__ uint32_t nco_counter(const NcoConst& nc, uint32_t base, int64_t w) {
+  const int64_t pv = (int64_t)base + w;
+  if (pv < 0) return (uint32_t)(pv + (int64_t)nc.rollover);
+  if (pv < 0x100000000LL) return fastmod_u32((uint32_t)pv, nc.fastmod, nc.rollover);
+  return (uint32_t)((uint64_t)pv % nc.rollover);
+}
+
+// e^{j 2 pi t} for t in 2^-64 turns, on the SFU: the reduced argument lies in
+// [-pi, pi), where __sincosf is accurate to ~4e-7 absolute.
+__device__ __forceinline__ float2 phasor64_fast(uint64_t turns64) {
   const int32_t top = (int32_t)(turns64 >> 32);
-  const float x = (float)top * 4.656612873077392578125e-10f;  // 2^-31: x in [-1, 1)
+  const float a = (float)top * 1.4629180792671596e-09f;  // 2 pi / 2^32
   float s, c;
-  sincospif(x, &s, &c);
+  __sincosf(a, &s, &c);
   return make_float2(c, s);
 }
 
+// Per (work set, channel) constants staged in shared memory by each CTA.
+struct ChanMeta {
+  uint64_t omega64, wrap64, fastmod;
+  float2* out;
+  uint32_t rollover, base, enabled, pad_;
+};
+
+// One row of one work set with NB live channels: T complex MACs per channel
+// (taps and samples from shared memory), then rotation and store.  Taps are
+// stored [T][NBS] with NBS = NB rounded up to even, so every row of taps
+// starts on a 16-byte boundary for the float4 loads.
 template <int NB>
-__device__ __forceinline__ void load_taps(const float2* __restrict__ p, float2 (&g)[NB]) {
-  if constexpr (NB == 1) {
-    g[0] = __ldg(p);
-  } else {
-    const float4* q = reinterpret_cast<const float4*>(p);
+__device__ __forceinline__ void process_row(const float2* __restrict__ xs, const float2* __restrict__ tp,
+                                            const ChanMeta* __restrict__ meta, int T, int D, int P, int a0, int jl,
+                                            int64_t j, int U, int r, int delta) {
+  constexpr int NBS = (NB + 1) & ~1;  // tap row stride (even: 16-byte aligned rows)
+  int bq = a0 / D;
+  int b = a0 - bq * D;
+  const float2* xp = xs + b * P + bq + jl;
+  const int wrap = 1 - D * P;
+  // Narrow batches keep the two products of each complex MAC in separate
+  // accumulators so the FMA dependency chains stay short.
+  constexpr bool kSplit = NB <= 4;
+  float2 acc[NB], acc2[kSplit ? NB : 1];
+#pragma unroll
+  for (int n = 0; n < NB; ++n) acc[n] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int n = 0; n < (kSplit ? NB : 1); ++n) acc2[n] = make_float2(0.f, 0.f);
+#pragma unroll 2
+  for (int k = 0; k < T; ++k) {
+    const float2 x = *xp;
+    float2 gk[NB];
+    const float4* q4 = reinterpret_cast<const float4*>(tp + k * NBS);
 #pragma unroll
     for (int i = 0; i < NB / 2; ++i) {
-      const float4 v = __ldg(q + i);
-      g[2 * i] = make_float2(v.x, v.y);
-      g[2 * i + 1] = make_float2(v.z, v.w);
+      const float4 v = q4[i];
+      gk[2 * i] = make_float2(v.x, v.y);
+      gk[2 * i + 1] = make_float2(v.z, v.w);
     }
-  }
-}
-
-// One CTA = one (decimation group, tile of Qt output rows).
-template <int NB>
-__global__ void __launch_bounds__(kThreads) poly_fp32_kernel(const __grid_constant__ PolyLaunch<NB> L) {
-  extern __shared__ float2 xs[];
-  const int g = blockIdx.x % L.ngroups;
-  const int tile = blockIdx.x / L.ngroups;
-  const GroupDesc& G = L.groups[g];
-  if (tile >= G.ntiles) return;
-  const int D = G.D, Qt = G.Qt, P = G.P;
-  const int64_t row0 = (int64_t)tile * Qt;
-  const int64_t sb = row0 * D + G.delta_min - G.tmax + 1;  // first staged input (block relative)
-  const int len = Qt * D + G.delta_span + G.tmax - 1;
-
-  // Stage the raw input span, de-interleaved by D.  Negative indices come from
-  // the history (the H samples before the block); past the block end is zero.
-  for (int t = threadIdx.x; t < len; t += blockDim.x) {
-    const int64_t v = sb + t;
-    float2 val = make_float2(0.f, 0.f);
-    if (v < 0) {
-      const int64_t hv = v + L.H;
-      if (hv >= 0) val = L.hist[hv];
-    } else if (v < L.N) {
-      val = L.block[v];
-    }
-    const int q = t / D;
-    xs[(t - q * D) * P + q] = val;
-  }
-  __syncthreads();
-
-  const int nitems = (G.ws_end - G.ws_begin) * Qt;
-  for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
-    const int wq = it / Qt;
-    const int jl = it - wq * Qt;
-    const WorkSet<NB>& W = L.ws[G.ws_begin + wq];
-    const int64_t j = row0 + jl;
-    if (j >= W.J) continue;
-    const int T = W.T;
-    const int a0 = (W.delta - G.delta_min) + (G.tmax - T);
-    int bq = a0 / D;
-    int b = a0 - bq * D;
-    int q = bq + jl;
-
-    float2 acc[NB];
+    if constexpr (NB & 1) gk[NB - 1] = tp[k * NBS + NB - 1];
 #pragma unroll
-    for (int n = 0; n < NB; ++n) acc[n] = make_float2(0.f, 0.f);
-
-    const float2* __restrict__ tp = W.taps;
-    for (int k = 0; k < T; ++k) {
-      const float2 x = xs[b * P + q];
-      float2 gk[NB];
-      load_taps<NB>(tp + (size_t)k * NB, gk);
-#pragma unroll
-      for (int n = 0; n < NB; ++n) {
+    for (int n = 0; n < NB; ++n) {
+      if constexpr (kSplit) {
+        acc[n].x = fmaf(gk[n].x, x.x, acc[n].x);
+        acc2[n].x = fmaf(-gk[n].y, x.y, acc2[n].x);
+        acc[n].y = fmaf(gk[n].x, x.y, acc[n].y);
+        acc2[n].y = fmaf(gk[n].y, x.x, acc2[n].y);
+      } else {
         acc[n].x = fmaf(gk[n].x, x.x, acc[n].x);
         acc[n].x = fmaf(-gk[n].y, x.y, acc[n].x);
         acc[n].y = fmaf(gk[n].x, x.y, acc[n].y);
         acc[n].y = fmaf(gk[n].y, x.x, acc[n].y);
       }
-      if (++b == D) {
-        b = 0;
-        ++q;
-      }
     }
+    xp += P;
+    if (++b == D) {
+      b = 0;
+      xp += wrap;
+    }
+  }
 
-    // Epilogue: rotate by the NCO phase of the window start, fix rollover
-    // straddles, store.
-    const int64_t m = (int64_t)W.r + (int64_t)W.U * j;
-    const int64_t w = (int64_t)W.delta + j * D - T + 1;  // window start, block relative
+  if constexpr (kSplit) {
 #pragma unroll
     for (int n = 0; n < NB; ++n) {
-      if (n >= W.nb) break;
-      const int c = W.ch[n];
-      float2 y = acc[n];
-      const NcoConst nc = L.nco[c];
-      if (nc.enabled) {
-        const uint32_t R = nc.rollover;
-        const int64_t pv = (int64_t)L.nco_base[c] + w;
-        uint64_t p;
-        if (pv < 0) {
-          p = (uint64_t)(pv + (int64_t)R);
-        } else if (pv < 0x100000000LL) {
-          p = (uint32_t)pv % R;
-        } else {
-          p = (uint64_t)pv % R;
-        }
-        const uint64_t ph = p * nc.omega64;
-        const float2 e = phasor64(ph);
-        if (p + (uint64_t)T - 1 >= (uint64_t)R) {
-          // The window crosses the counter rollover: samples from k0 on use
-          // angle w*(p + k - R) instead of w*(p + k).
-          const int k0 = (int)((uint64_t)R - p);
-          float2 B = make_float2(0.f, 0.f);
-          int kb = a0 + k0;
-          int qq = kb / D;
-          int bb = kb - qq * D;
-          qq += jl;
-          for (int k = k0; k < T; ++k) {
-            const float2 x = xs[bb * P + qq];
-            const float2 gk = __ldg(tp + (size_t)k * NB + n);
-            B.x = fmaf(gk.x, x.x, B.x);
-            B.x = fmaf(-gk.y, x.y, B.x);
-            B.y = fmaf(gk.x, x.y, B.y);
-            B.y = fmaf(gk.y, x.x, B.y);
-            if (++bb == D) {
-              bb = 0;
-              ++qq;
-            }
-          }
-          const float2 e2 = phasor64(ph - nc.wrap64);
-          const float2 A = make_float2(y.x - B.x, y.y - B.y);
-          const float2 ya = cmul(A, e), yb = cmul(B, e2);
-          y = make_float2(ya.x + yb.x, ya.y + yb.y);
-        } else {
-          y = cmul(y, e);
-        }
+      acc[n].x += acc2[n].x;
+      acc[n].y += acc2[n].y;
+    }
+  }
+
+  // Epilogue: rotate by the NCO phase of the window start, fix rollover
+  // straddles, store.
+  const int64_t m = (int64_t)r + (int64_t)U * j;
+  const int64_t w = (int64_t)delta + j * D - T + 1;  // window start, block relative
+#pragma unroll
+  for (int n = 0; n < NB; ++n) {
+    const ChanMeta& cm = meta[n];
+    float2 y = acc[n];
+    if (cm.enabled) {
+      const uint32_t R = cm.rollover;
+      const int64_t pv = (int64_t)cm.base + w;
+      uint32_t p;
+      if (pv < 0) {
+        p = (uint32_t)(pv + (int64_t)R);
+      } else if (pv < 0x100000000LL) {
+        p = fastmod_u32((uint32_t)pv, cm.fastmod, R);
+      } else {
+        p = (uint32_t)((uint64_t)pv % R);
       }
-      L.out[c][m] = y;
+      const uint64_t ph = (uint64_t)p * cm.omega64;
+      const float2 e = phasor64_fast(ph);
+      if ((uint64_t)p + (uint64_t)T - 1 >= (uint64_t)R) {
+        // The window crosses the counter rollover: samples from k0 on use
+        // angle w*(p + k - R) instead of w*(p + k).
+        const int k0 = (int)(R - p);
+        float2 B = make_float2(0.f, 0.f);
+        const int kb = a0 + k0;
+        int qq = kb / D;
+        int bb = kb - qq * D;
+        qq += jl;
+        for (int k = k0; k < T; ++k) {
+          const float2 x = xs[bb * P + qq];
+          const float2 gk = tp[k * NBS + n];
+          B.x = fmaf(gk.x, x.x, B.x);
+          B.x = fmaf(-gk.y, x.y, B.x);
+          B.y = fmaf(gk.x, x.y, B.y);
+          B.y = fmaf(gk.y, x.x, B.y);
+          if (++bb == D) {
+            bb = 0;
+            ++qq;
+          }
+        }
+        const float2 e2 = phasor64_fast(ph - cm.wrap64);
+        const float2 A = make_float2(y.x - B.x, y.y - B.y);
+        const float2 ya = cmul(A, e), yb = cmul(B, e2);
+        y = make_float2(ya.x + yb.x, ya.y + yb.y);
+      } else {
+        y = cmul(y, e);
+      }
+    }
+    cm.out[m] = y;
+  }
+}
+
+// One CTA = one tile of Qt output rows of decimation group g.  Shared memory:
+// [input tile, de-interleaved: D x P float2][taps of every work set of the
+// group, packed [T][nb]][ChanMeta per (work set, channel)].
+template <int NBMAX, bool kTapsSmem>
+__global__ void __launch_bounds__(kThreads, 3) poly_fp32_kernel(const __grid_constant__ PolyLaunch<NBMAX> L, int g) {
+  extern __shared__ __align__(16) float2 xs[];
+  const GroupDesc& G = L.groups[g];
+  const int tile = blockIdx.x;
+  const int D = G.D, Qt = G.Qt, P = G.P;
+  const int64_t row0 = (int64_t)tile * Qt;
+  const int64_t sb = row0 * D + G.delta_min - G.tmax + 1;  // first staged input (block relative)
+  const int len = Qt * D + G.delta_span + G.tmax - 1;
+  float2* taps_s = xs + G.taps_off;
+  ChanMeta* meta_s = reinterpret_cast<ChanMeta*>(xs + G.meta_off);
+  const int nws = G.ws_end - G.ws_begin;
+
+  // Stage the raw input span, de-interleaved by D, with asynchronous 8-byte
+  // copies (every copy of the tile in flight at once).  Negative indices come
+  // from the history (the H samples before the block); past the block end the
+  // copy reads 0 bytes and zero-fills.
+  for (int t = threadIdx.x; t < len; t += blockDim.x) {
+    const int64_t v = sb + t;
+    const float2* src = L.block;
+    uint32_t bytes = 0;
+    if (v < 0) {
+      const int64_t hv = v + L.H;
+      if (hv >= 0) {
+        src = L.hist + hv;
+        bytes = 8;
+      }
+    } else if (v < L.N) {
+      src = L.block + v;
+      bytes = 8;
+    }
+    const int q = t / D;
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(xs + (t - q * D) * P + q);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  // Stage the taps of every work set (when they fit) and the per-channel NCO
+  // constants.
+  for (int wi = 0; wi < nws; ++wi) {
+    const WorkSet<NBMAX>& W = L.ws[G.ws_begin + wi];
+    if constexpr (kTapsSmem) {
+      const int cnt = W.T * ((W.nb + 1) & ~1);
+      for (int i = threadIdx.x; i < cnt; i += blockDim.x) taps_s[W.soff + i] = __ldg(W.taps + i);
+    }
+    if (threadIdx.x < W.nb) {
+      const int c = W.ch[threadIdx.x];
+      const NcoConst nc = L.nco[c];
+      ChanMeta m;
+      m.omega64 = nc.omega64;
+      m.wrap64 = nc.wrap64;
+      m.fastmod = nc.fastmod;
+      m.out = L.out[c];
+      m.rollover = nc.rollover;
+      m.base = L.nco_base[c];
+      m.enabled = nc.enabled;
+      m.pad_ = 0;
+      meta_s[wi * NBMAX + threadIdx.x] = m;
+    }
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
+
+  // Items are (work set, row) with rows fastest; Qt is a multiple of 32 so a
+  // warp never mixes work sets and every tap load is a broadcast.
+  const int nitems = nws * Qt;
+  for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+    const int wq = it / Qt;
+    const int jl = it - wq * Qt;
+    const WorkSet<NBMAX>& W = L.ws[G.ws_begin + wq];
+    const int64_t j = row0 + jl;
+    if (j >= W.J) continue;
+    const int T = W.T;
+    const int a0 = (W.delta - G.delta_min) + (G.tmax - T);
+    const float2* tp = kTapsSmem ? taps_s + W.soff : W.taps;
+    const ChanMeta* mt = meta_s + wq * NBMAX;
+    switch (W.nb) {
+      case 1: process_row<1>(xs, tp, mt, T, D, P, a0, jl, j, W.U, W.r, W.delta); break;
+      case 2: if constexpr (NBMAX >= 2) process_row<2>(xs, tp, mt, T, D, P, a0, jl, j, W.U, W.r, W.delta); break;
+      case 3: if constexpr (NBMAX >= 3) process_row<3>(xs, tp, mt, T, D, P, a0, jl, j, W.U, W.r, W.delta); break;
+      case 4: if constexpr (NBMAX >= 4) process_row<4>(xs, tp, mt, T, D, P, a0, jl, j, W.U, W.r, W.delta); break;
+      case 5: if constexpr (NBMAX >= 5) process_row<5>(xs, tp, mt, T, D, P, a0, jl, j, W.U, W.r, W.delta); break;
+      case 6: if constexpr (NBMAX >= 6) process_row<6>(xs, tp, mt, T, D, P, a0, jl, j, W.U, W.r, W.delta); break;
+      case 7: if constexpr (NBMAX >= 7) process_row<7>(xs, tp, mt, T, D, P, a0, jl, j, W.U, W.r, W.delta); break;
+      default: if constexpr (NBMAX >= 8) process_row<NBMAX>(xs, tp, mt, T, D, P, a0, jl, j, W.U, W.r, W.delta); break;
     }
   }
 }
@@ -214,6 +307,7 @@ NcoConst make_nco(uint32_t fs, int32_t f) {
   n.omega64 = w;
   n.wrap64 = (uint64_t)R * w;
   n.rollover = R;
+  n.fastmod = R ? (~0ull / R + 1) : 0;
   n.enabled = (R != 0) ? 1u : 0u;
   return n;
 }
@@ -229,9 +323,9 @@ PolyEngine::~PolyEngine() {
 }
 
 static int choose_qt(uint32_t D, int tmax) {
-  // ~8K input samples per tile, at least one warp of rows, shared memory
-  // (tile + halo + offset spread, de-interleaved) under ~200 KB.
-  int qt = (int)((8192 / D) & ~31u);
+  // ~4K input samples per tile (three CTAs per SM), at least one warp of rows,
+  // shared memory (tile + halo + offset spread, de-interleaved) under ~200 KB.
+  int qt = (int)((4096 / D) & ~31u);
   if (qt < 32) qt = 32;
   auto bytes = [&](int q) {
     const int64_t len = (int64_t)q * D + 3LL * D + tmax;
@@ -339,7 +433,8 @@ int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool
   // modulated, padded taps of every batch: [up][T][NB]
   for (auto& bt : batches_) {
     const uint32_t U = classes_[bt.cls].up;
-    std::vector<float2> host((size_t)U * bt.T * nb_, make_float2(0.f, 0.f));
+    const size_t nb = (bt.chans.size() + 1) & ~(size_t)1;  // tap rows padded to an even width
+    std::vector<float2> host((size_t)U * bt.T * nb, make_float2(0.f, 0.f));
     for (size_t n = 0; n < bt.chans.size(); ++n) {
       const EngineChannel& e = chans_[bt.chans[n]];
       const int pad = bt.T - (int)e.T;
@@ -360,7 +455,7 @@ int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool
             gr = (double)h.x * c - (double)h.y * s;
             gi = (double)h.x * s + (double)h.y * c;
           }
-          host[((size_t)ph * bt.T + k) * nb_ + n] = make_float2((float)gr, (float)gi);
+          host[((size_t)ph * bt.T + k) * nb + n] = make_float2((float)gr, (float)gi);
         }
       }
     }
@@ -468,7 +563,7 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
         const uint32_t phi = (uint32_t)(t % U);
         if (nws >= kMaxWorkSets) return FDSP_ERR_UNSUPPORTED;
         WorkSet<NB>& W = L.ws[nws++];
-        W.taps = bt.d_taps + (size_t)phi * bt.T * NB;
+        W.taps = bt.d_taps + (size_t)phi * bt.T * ((bt.chans.size() + 1) & ~(size_t)1);
         W.T = bt.T;
         W.delta = (int32_t)delta;
         W.J = (int32_t)J;
@@ -492,7 +587,24 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
     int64_t P = (len + g.D - 1) / g.D;
     if ((P & 1) == 0) P++;  // odd pitch: the staging scatter spreads over banks
     gd.P = (int32_t)P;
-    smem_max = std::max(smem_max, (size_t)(g.D * P * sizeof(float2)));
+    // shared-memory layout: input tile | taps of each work set | channel constants
+    int64_t off = ((int64_t)g.D * P + 1) & ~1LL;  // float2 units, 16-byte aligned
+    gd.taps_off = (int32_t)off;
+    int64_t toff = 0;
+    for (int wi = gd.ws_begin; wi < gd.ws_end; ++wi) {
+      L.ws[wi].soff = (int32_t)toff;
+      toff += (int64_t)L.ws[wi].T * ((L.ws[wi].nb + 1) & ~1);
+    }
+    const int64_t meta_bytes = (int64_t)(gd.ws_end - gd.ws_begin) * NB * 48;
+    // taps go to shared memory unless they would push the CTA past ~150 KB
+    // (long filters of many phases); those groups read taps through L1
+    gd.taps_smem = ((off + toff) * (int64_t)sizeof(float2) + meta_bytes <= 150 * 1024) ? 1 : 0;
+    if (gd.taps_smem) off += toff;
+    gd.meta_off = (int32_t)off;
+    const int64_t bytes = off * (int64_t)sizeof(float2) + meta_bytes;
+    if (bytes > 227 * 1024) return FDSP_ERR_UNSUPPORTED;
+    gd.smem_bytes = (int32_t)bytes;
+    smem_max = std::max(smem_max, (size_t)bytes);
     max_tiles = std::max(max_tiles, gd.ntiles);
     ng++;
   }
@@ -500,14 +612,16 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
   L.max_tiles = max_tiles;
   L.nws = nws;
   launches_last_ = 0;
-  if (ng > 0 && max_tiles > 0) {
-    if (smem_max > 227 * 1024) return FDSP_ERR_UNSUPPORTED;
-    cudaError_t e = cudaFuncSetAttribute(poly_fp32_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem_max);
+  // one launch per decimation group, each with its own tile shape and
+  // shared-memory size (all on `stream`, so they run back to back)
+  for (int gi = 0; gi < ng; ++gi) {
+    const GroupDesc& gd = L.groups[gi];
+    if (gd.ntiles <= 0) continue;
+    const size_t smem = (size_t)gd.smem_bytes;
+    auto kern = gd.taps_smem ? poly_fp32_kernel<NB, true> : poly_fp32_kernel<NB, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e);
-    const int64_t nblocks = (int64_t)ng * max_tiles;
-    if (nblocks > 0x7fffffffLL) return FDSP_ERR_UNSUPPORTED;
-    poly_fp32_kernel<NB><<<(unsigned)nblocks, kThreads, smem_max, stream>>>(L);
+    kern<<<(unsigned)gd.ntiles, kThreads, smem, stream>>>(L, gi);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;

@@ -30,6 +30,7 @@ constexpr int kThreads = 256;       // threads per CTA of the FP32 engine kernel
 struct NcoConst {
   uint64_t omega64;   // turns per sample, 2^-64 units
   uint64_t wrap64;    // R * omega64 mod 2^64 (phase that the rollover drops)
+  uint64_t fastmod;   // ceil(2^64 / R): n mod R as one 64-bit multiply-high
   uint32_t rollover;  // R; 0 when the channel has no shift
   uint32_t enabled;   // 0: phasor is exactly 1 (shift of 0 Hz)
 };
@@ -45,7 +46,10 @@ struct GroupDesc {
   int32_t ntiles;     // tiles of Qt rows in this launch
   int32_t ws_begin;   // work sets [ws_begin, ws_end) belong to this group
   int32_t ws_end;
-  int32_t pad_;
+  int32_t taps_off;   // shared-memory offset (float2) of the staged taps
+  int32_t meta_off;   // shared-memory offset (float2) of the staged channel constants
+  int32_t smem_bytes; // dynamic shared memory of one CTA
+  int32_t taps_smem;  // 1: taps staged in shared memory; 0: read through L1
 };
 
 // One (tap batch, output class r) pair of a launch.  Output j of the class is
@@ -53,8 +57,9 @@ struct GroupDesc {
 // [delta + j*D - T + 1, delta + j*D] in block-relative input indices.
 template <int NB>
 struct WorkSet {
-  const float2* taps;   // [T][NB] modulated taps of phase phi_r
+  const float2* taps;   // [T][nb] modulated taps of phase phi_r (device)
   int32_t T;            // padded taps per phase of the batch
+  int32_t soff;         // shared-memory offset (float2) of these taps in the CTA
   int32_t delta;        // window end of row j = 0 (block relative)
   int32_t J;            // rows that have an output in this launch
   int32_t U;            // up rate of the batch's channels
@@ -108,7 +113,7 @@ struct EngineBatch {
   int group;           // decimation group index
   int T;               // padded taps per phase
   std::vector<int> chans;
-  float2* d_taps;      // [up][T][NB] on the device
+  float2* d_taps;      // [up][T][nb] on the device
 };
 
 struct EngineGroup {
@@ -139,7 +144,7 @@ class PolyEngine {
   uint64_t samples_since_reset() const { return abs0_; }
   int history_len() const { return H_; }
   int nb() const { return nb_; }
-  // Test/diagnostic hook: force the FP32 kernel's NB template (1,2,4,8).
+  // Kernel launches enqueued by the most recent apply.
   int kernel_launches_last() const { return launches_last_; }
 
  private:

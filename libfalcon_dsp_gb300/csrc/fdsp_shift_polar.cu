@@ -13,11 +13,13 @@
 
 namespace fdsp {
 
+// e^{j 2 pi t} for t in 2^-64 turns; the argument handed to the SFU lies in
+// [-pi, pi), where __sincosf is accurate to ~4e-7 absolute.
 __device__ __forceinline__ float2 phasor64_sp(uint64_t turns64) {
   const int32_t top = (int32_t)(turns64 >> 32);
-  const float x = (float)top * 4.656612873077392578125e-10f;
+  const float a = (float)top * 1.4629180792671596e-09f;  // 2 pi / 2^32
   float s, c;
-  sincospif(x, &s, &c);
+  __sincosf(a, &s, &c);
   return make_float2(c, s);
 }
 
