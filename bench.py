@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=1 << 20, help="input samples of the CPU baseline sample")
+    ap.add_argument("--precision", default="fp16x3", choices=["fp32", "fp16x3", "bf16x3"],
+                    help="filter-bank arithmetic of the headline number (tensor-core split forms or plain FP32)")
+    ap.add_argument("--no-fp32-compare", action="store_true")
     return ap.parse_args()
 
 
@@ -212,6 +215,7 @@ def run_ours(args) -> None:
 
     x, fs, chans = channelizer_256(args.n, SEED, device=dev)
     ch = F.MultiRateChannelizerCuda(fs, chans)
+    ch.set_precision(args.precision)
     nch = len(chans)
     stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
@@ -257,6 +261,24 @@ def run_ours(args) -> None:
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
+
+    # the plain FP32 form of the same step, timed the same way, for comparison
+    plain = None
+    if args.precision != "fp32" and not args.no_fp32_compare:
+        ch.set_precision("fp32")
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        fo = 0
+        for _ in range(args.steps):
+            fo += step()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fms = f0.elapsed_time(f1)
+        plain = {"value": round(fo / (fms / 1e3) / 1e6, 1), "unit": "Msamples/s", "ms_per_step": round(fms / args.steps, 4)}
+        ch.set_precision(args.precision)
     if world > 1:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -273,11 +295,13 @@ def run_ours(args) -> None:
     bytes_per_launch = algorithmic_bytes(x.numel(), outputs // args.steps)
     achieved_gbs = bytes_per_launch / (ms_per_step / 1e3) / 1e9
     pk = peaks()
-    traffic = ncu_traffic("poly_fp32_kernel_channelizer_256", x.numel())
+    kname = "poly_fp32_kernel" if args.precision == "fp32" else "poly_tc_kernel"
+    traffic = ncu_traffic(f"{kname}_channelizer_256", x.numel())
     roof = {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved_gbs / pk["hbm_gbs"], 4), "traffic": traffic,
-            "kernel": "poly_fp32_kernel", "peak_source": pk["source"],
-            "bytes_per_launch": bytes_per_launch}
+            "kernel": kname, "peak_source": pk["source"],
+            "bytes_per_launch": bytes_per_launch,
+            "note": "one step = one launch per decimation group (12) + one history update; achieved uses the step time"}
 
     # end to end through the host-buffer C ABI call (pinned host memory)
     e2e = None
@@ -329,12 +353,18 @@ def run_ours(args) -> None:
         line = {
             "metric": "channelizer output Msamples/s", "value": round(value, 1), "unit": "Msamples/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_in": x.numel(), "channels": nch, "seed": SEED, "path": "plain FP32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32" if args.precision == "fp32" else args.precision + "(fp32 accumulate)",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_in": x.numel(), "channels": nch, "seed": SEED,
+                       "path": {"fp32": "plain FP32 SIMT", "fp16x3": "tensor cores (tcgen05), FP16 hi+lo x3",
+                                "bf16x3": "tensor cores (tcgen05), BF16 hi+lo x3"}[args.precision],
                        "l2": "no flush: each step reads 512 MiB and writes ~9.6 GB, far above the 129 MB L2",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_step * args.steps,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "plain_fp32": plain,
+            "tc_speedup_vs_plain_fp32": round(ms_per_step / plain["ms_per_step"], 3) ** -1 if plain else None,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -102,6 +102,13 @@ typedef struct {
 
 typedef struct fdsp_channelizer fdsp_channelizer;
 
+/* Arithmetic of the channelizer's filter-bank contraction. */
+enum fdsp_precision {
+    FDSP_PRECISION_FP32 = 0,     /* plain FP32 complex arithmetic on the SIMT cores (default) */
+    FDSP_PRECISION_FP16X3 = 1,   /* tensor cores: FP16 hi+lo split of data and taps, 3 products, FP32 accumulate */
+    FDSP_PRECISION_BF16X3 = 2    /* tensor cores: BF16 hi+lo split, 3 products, FP32 accumulate */
+};
+
 /* initialize(input_sample_rate, channels)
  * (src/transform/falcon_dsp_multi_rate_channelizer_cuda.cu:320-372). */
 int fdsp_channelizer_create(uint32_t input_sample_rate, const fdsp_channel_cfg *channels, uint32_t num_channels,
@@ -116,6 +123,9 @@ int fdsp_channelizer_out_count(const fdsp_channelizer *h, uint64_t n_in, uint64_
  * NULL to skip the check) receives n_out[c] samples. */
 int fdsp_channelizer_apply(fdsp_channelizer *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *const *d_out,
                            const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);
+/* Select the arithmetic of later applies (fdsp_precision).  Channels whose
+ * taps per phase exceed 64 keep the FP32 form in the tensor-core modes. */
+int fdsp_channelizer_set_precision(fdsp_channelizer *h, int precision);
 /* Kernel launches the most recent apply enqueued (diagnostics, profiling). */
 int fdsp_channelizer_kernel_launches(const fdsp_channelizer *h, uint32_t *n);
 /* apply(in, out) on host buffers (copies in, computes, copies out, syncs). */

@@ -147,6 +147,18 @@ class MultiRateChannelizerCuda(_Handle):
         _capi.call("fdsp_channelizer_out_count", self._h, int(n_in), out)
         return list(out)
 
+    PRECISION = {"fp32": 0, "fp16x3": 1, "bf16x3": 2}
+
+    def set_precision(self, mode: str = "fp32") -> None:
+        """'fp32' (SIMT FP32, default), or the tensor-core split-precision forms
+        'fp16x3' / 'bf16x3' (hi+lo operands, 3 products, FP32 accumulation)."""
+        _capi.call("fdsp_channelizer_set_precision", self._h, self.PRECISION[mode])
+
+    def kernel_launches(self) -> int:
+        v = C.c_uint32()
+        _capi.call("fdsp_channelizer_kernel_launches", self._h, C.byref(v))
+        return v.value
+
     def reset_state(self) -> None:
         _capi.call("fdsp_channelizer_reset", self._h)
 

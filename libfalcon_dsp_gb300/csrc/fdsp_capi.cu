@@ -228,6 +228,11 @@ int fdsp_channelizer_apply(fdsp_channelizer* h, const fdsp_cf32* d_in, uint64_t 
                       n_out, (cudaStream_t)stream);
 }
 
+int fdsp_channelizer_set_precision(fdsp_channelizer* h, int precision) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return h->eng.set_precision(precision);
+}
+
 int fdsp_channelizer_kernel_launches(const fdsp_channelizer* h, uint32_t* n) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
   if (!n) return FDSP_ERR_INVALID_ARG;

@@ -32,6 +32,7 @@
 #include <map>
 
 #include "fdsp_internal.h"
+#include "fdsp_nco.cuh"
 
 namespace fdsp {
 
@@ -66,12 +67,7 @@ __device__ __forceinline__ float2 phasor64_fast(uint64_t turns64) {
   return make_float2(c, s);
 }
 
-// Per (work set, channel) constants staged in shared memory by each CTA.
-struct ChanMeta {
-  uint64_t omega64, wrap64, fastmod;
-  float2* out;
-  uint32_t rollover, base, enabled, pad_;
-};
+using ChanMeta = OutMeta;
 
 // One row of one work set with NB live channels: T complex MACs per channel
 // (taps and samples from shared memory), then rotation and store.  Taps are
@@ -135,57 +131,47 @@ __device__ __forceinline__ void process_row(const float2* __restrict__ xs, const
     }
   }
 
-  // Epilogue: rotate by the NCO phase of the window start, fix rollover
-  // straddles, store.
+  // Epilogue: rotate by the NCO phase of the window start (branch free, so
+  // the channels' phase chains interleave), store; windows that straddle the
+  // NCO rollover take the exact split-sum path.
   const int64_t m = (int64_t)r + (int64_t)U * j;
   const int64_t w = (int64_t)delta + j * D - T + 1;  // window start, block relative
+  // The rare outputs that need the exact path (window across the NCO
+  // rollover) are first written unrotated, then fixed from that value, so no
+  // accumulator stays live through the fix-up.
+  uint32_t slow = 0;
 #pragma unroll
   for (int n = 0; n < NB; ++n) {
-    const ChanMeta& cm = meta[n];
     float2 y = acc[n];
-    if (cm.enabled) {
-      const uint32_t R = cm.rollover;
-      const int64_t pv = (int64_t)cm.base + w;
-      uint32_t p;
-      if (pv < 0) {
-        p = (uint32_t)(pv + (int64_t)R);
-      } else if (pv < 0x100000000LL) {
-        p = fastmod_u32((uint32_t)pv, cm.fastmod, R);
-      } else {
-        p = (uint32_t)((uint64_t)pv % R);
-      }
-      const uint64_t ph = (uint64_t)p * cm.omega64;
-      const float2 e = phasor64_fast(ph);
-      if ((uint64_t)p + (uint64_t)T - 1 >= (uint64_t)R) {
-        // The window crosses the counter rollover: samples from k0 on use
-        // angle w*(p + k - R) instead of w*(p + k).
-        const int k0 = (int)(R - p);
-        float2 B = make_float2(0.f, 0.f);
-        const int kb = a0 + k0;
-        int qq = kb / D;
-        int bb = kb - qq * D;
-        qq += jl;
-        for (int k = k0; k < T; ++k) {
-          const float2 x = xs[bb * P + qq];
-          const float2 gk = tp[k * NBS + n];
-          B.x = fmaf(gk.x, x.x, B.x);
-          B.x = fmaf(-gk.y, x.y, B.x);
-          B.y = fmaf(gk.x, x.y, B.y);
-          B.y = fmaf(gk.y, x.x, B.y);
-          if (++bb == D) {
-            bb = 0;
-            ++qq;
-          }
+    const bool ok = rotate_fast(meta[n], w, T, y);
+    meta[n].out[m] = ok ? y : acc[n];
+    slow |= ok ? 0u : (1u << n);
+  }
+  while (slow) {
+    const int n = __ffs(slow) - 1;
+    slow &= slow - 1;
+    const OutMeta& cm = meta[n];
+    const ExactRot er = rotate_prep(cm, w, T);
+    float2 B = make_float2(0.f, 0.f);
+    if (er.straddle) {
+      const int kb = a0 + er.k0;
+      int qq = kb / D;
+      int bb = kb - qq * D;
+      qq += jl;
+      for (int k = er.k0; k < T; ++k) {
+        const float2 x = xs[bb * P + qq];
+        const float2 gk = tp[k * NBS + n];
+        B.x = fmaf(gk.x, x.x, B.x);
+        B.x = fmaf(-gk.y, x.y, B.x);
+        B.y = fmaf(gk.x, x.y, B.y);
+        B.y = fmaf(gk.y, x.x, B.y);
+        if (++bb == D) {
+          bb = 0;
+          ++qq;
         }
-        const float2 e2 = phasor64_fast(ph - cm.wrap64);
-        const float2 A = make_float2(y.x - B.x, y.y - B.y);
-        const float2 ya = cmul(A, e), yb = cmul(B, e2);
-        y = make_float2(ya.x + yb.x, ya.y + yb.y);
-      } else {
-        y = cmul(y, e);
       }
     }
-    cm.out[m] = y;
+    cm.out[m] = rotate_apply(er, cm.out[m], B);
   }
 }
 
@@ -313,6 +299,7 @@ NcoConst make_nco(uint32_t fs, int32_t f) {
 }
 
 PolyEngine::~PolyEngine() {
+  free_tc();
   for (auto& b : batches_) {
     if (b.d_taps) cudaFree(b.d_taps);
   }
@@ -423,6 +410,7 @@ int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool
       batches_.push_back(bt);
     }
   }
+  for (size_t gi = 0; gi < groups_.size(); ++gi) group_of_d_[groups_[gi].D] = (int)gi;
   for (auto& g : groups_) {
     int tmax = 1;
     for (int b : g.batches) tmax = std::max(tmax, batches_[b].T);
@@ -514,7 +502,21 @@ int PolyEngine::out_counts(uint64_t n_in, uint64_t* n_out) const {
   return FDSP_OK;
 }
 
+int PolyEngine::set_precision(int mode) {
+  if (mode == precision_) return FDSP_OK;
+  if (mode == FDSP_PRECISION_FP32) {
+    precision_ = mode;
+    return FDSP_OK;
+  }
+  if (mode != FDSP_PRECISION_FP16X3 && mode != FDSP_PRECISION_BF16X3) return FDSP_ERR_INVALID_ARG;
+  const int st = build_tc(mode == FDSP_PRECISION_FP16X3 ? 0 : 1);
+  if (st != FDSP_OK) return st;
+  precision_ = mode;
+  return FDSP_OK;
+}
+
 void PolyEngine::reset() {
+  if (d_err_) cudaMemset(d_err_, 0, sizeof(int));
   for (auto& k : classes_) {
     k.phase = 0;
     k.xoffset = 0;
@@ -611,12 +613,30 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
   L.ngroups = ng;
   L.max_tiles = max_tiles;
   L.nws = nws;
-  launches_last_ = 0;
+  // tensor-core groups read the input pre-split into {hi, lo} pairs
+  if (precision_ != FDSP_PRECISION_FP32) {
+    bool any_tc = false;
+    for (int gi = 0; gi < ng; ++gi) any_tc = any_tc || group_tc_ok(group_of_d_[L.groups[gi].D]);
+    if (any_tc) {
+      const int st = prepare_tc_input(d_in, n, stream);
+      if (st != FDSP_OK) return st;
+    }
+  }
   // one launch per decimation group, each with its own tile shape and
   // shared-memory size (all on `stream`, so they run back to back)
   for (int gi = 0; gi < ng; ++gi) {
     const GroupDesc& gd = L.groups[gi];
     if (gd.ntiles <= 0) continue;
+    if (precision_ != FDSP_PRECISION_FP32) {
+      const int eg = group_of_d_[gd.D];
+      if (group_tc_ok(eg)) {
+        // groups whose operands do not fit the tensor-core kernel's shared
+        // memory keep the FP32 form (nothing was launched in that case)
+        const int st = launch_tc_group(eg, d_in, n, out, stream);
+        if (st == FDSP_OK) continue;
+        if (st != FDSP_ERR_UNSUPPORTED) return st;
+      }
+    }
     const size_t smem = (size_t)gd.smem_bytes;
     auto kern = gd.taps_smem ? poly_fp32_kernel<NB, true> : poly_fp32_kernel<NB, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -639,6 +659,7 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
 
 int PolyEngine::apply(const float2* d_in, uint64_t n, float2* const* out, const uint64_t* cap, uint64_t* n_out,
                       cudaStream_t stream) {
+  launches_last_ = 0;
   if (n > 0 && d_in == nullptr) return FDSP_ERR_INVALID_ARG;
   if (n >= (1ull << 31)) return FDSP_ERR_UNSUPPORTED;
   for (auto& k : classes_) k.M = class_out_count(k, n);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <vector>
 
 #include "fdsp_c.h"
@@ -84,6 +85,70 @@ struct PolyLaunch {
   uint32_t nco_base[kMaxChannels];   // (samples since reset at block[0]) mod R
 };
 
+// ---------------------------------------------------------------------------
+// Tensor-core launch (one decimation group per launch).
+// ---------------------------------------------------------------------------
+constexpr int kMaxTcWorkSets = 192;
+
+struct TcWorkSet {
+  const uint8_t* bhi;    // B hi part, tcgen05 K-major no-swizzle layout (device)
+  const uint8_t* blo;    // B lo part
+  const float2* taps32;  // [T][n] FP32 modulated taps (rollover correction)
+  const int16_t* ch;     // channel ids of the chunk (device)
+  int32_t T;             // padded taps per phase (multiple of 8, <= 64)
+  int32_t N_pad;         // MMA N = 2 n rounded up to 16
+  int32_t n;             // channels in the chunk
+  int32_t delta;         // window end of row 0 (block relative)
+  int32_t J;             // rows with an output in this launch
+  int32_t U;
+  int32_t r;
+  int32_t bbytes;        // bytes of one B part
+  int32_t ntiles;        // 128-row tiles of this work set
+  int32_t boff;          // shared-memory byte offset of this work set's B (hi, then lo)
+  int32_t moff;          // shared-memory byte offset of its channel constants
+  int32_t pad_;
+};
+
+struct TcGroup {
+  int32_t D, ws_begin, ws_end, ntiles;
+  int32_t in_off;        // shared-memory byte offset of the staged input
+  int32_t P;             // de-interleaved tile pitch (float2), tile-staging mode
+  int32_t tmax;          // longest padded window of the group
+  int32_t delta_min;     // smallest window-end offset of the group's work sets
+  int32_t delta_span;    // largest minus smallest
+  int32_t win_pitch;     // per-row window pitch (float2), window-staging mode
+  int32_t tile_elems;    // elements of one (double-buffered) de-interleaved tile
+};
+
+struct TcLaunch {
+  const float2* block;
+  const float2* hist;
+  const uint2* xhl;                  // [history | block] as packed {hi, lo} 16-bit pairs
+  int64_t N;
+  int32_t H;
+  int32_t ngroups;
+  const NcoConst* nco;
+  int* err;                          // set to 1 when a bounded wait gave up
+  TcGroup groups[kMaxGroups];
+  TcWorkSet ws[kMaxTcWorkSets];
+  float2* out[kMaxChannels];
+  uint32_t nco_base[kMaxChannels];
+};
+
+static_assert(sizeof(TcLaunch) <= 32764, "tensor-core launch must fit the kernel parameter block");
+
+struct TcChunk {
+  int cls;
+  std::vector<int> chans;
+  int T;          // padded taps per phase
+  bool supported; // T <= 64
+  int N_pad;
+  int bbytes;
+  uint8_t* d_b;   // [U][hi|lo][bbytes]
+  float2* d_taps32;
+  int16_t* d_ch;
+};
+
 // CUDA error -> status, remembering the CUDA code for fdsp_last_cuda_error().
 int cuda_status(cudaError_t e);
 void set_last_cuda_error(int code);
@@ -147,9 +212,29 @@ class PolyEngine {
   // Kernel launches enqueued by the most recent apply.
   int kernel_launches_last() const { return launches_last_; }
 
+  // Arithmetic of the filter-bank contraction: FDSP_PRECISION_FP32 (SIMT FP32)
+  // or one of the split-precision tensor-core forms.
+  int set_precision(int mode);
+  int precision() const { return precision_; }
+  // 1 when a tensor-core kernel hit its bounded wait since the last reset.
+  int tc_error() const;
+
  private:
   template <int NB>
   int launch(const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream);
+  int build_tc(int fmt);
+  void free_tc();
+  bool group_tc_ok(int gi) const;
+  int groups_idx_of_class(int cls) const;
+  int launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream);
+  int prepare_tc_input(const float2* d_in, uint64_t n, cudaStream_t stream);
+  uint2* d_xhl_ = nullptr;          // scratch: pre-split input of the current apply
+  size_t xhl_cap_ = 0;
+  int precision_ = FDSP_PRECISION_FP32;
+  int tc_fmt_ = 0;
+  std::vector<TcChunk> tc_chunks_;
+  int* d_err_ = nullptr;
+  int num_sms_ = 0;
 
   uint32_t fs_ = 0;
   bool complex_taps_ = false;
@@ -160,6 +245,7 @@ class PolyEngine {
   std::vector<int> cls_of_;
   std::vector<EngineBatch> batches_;
   std::vector<EngineGroup> groups_;
+  std::map<uint32_t, int> group_of_d_;
   NcoConst* d_nco_ = nullptr;
   float2* d_hist_[2] = {nullptr, nullptr};
   int hist_cur_ = 0;
