@@ -160,6 +160,36 @@ int fdsp_resampler_apply_host(fdsp_resampler *h, const fdsp_cf32 *h_in, uint64_t
                               uint64_t out_cap, uint64_t *n_out, fdsp_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * One-shot polyphase resampling that allocates nothing.
+ * No counterpart in the reference: it is the result of
+ * fdsp_resampler_create + fdsp_resampler_apply + fdsp_resampler_destroy on a
+ * fresh resampler (same output count, outputs equal within FP32 rounding),
+ * for callers that may not allocate once they run: real-time receive loops,
+ * where a cudaMalloc/cudaFree would synchronise the device and stall the
+ * other streams, and plug-ins whose host owns the device-memory budget.
+ *
+ *   - The taps go into one fixed device array of
+ *     FDSP_RESAMPLE_STATIC_MAX_COEFFS complex values (64 KiB) per device;
+ *     num_coeffs above that returns FDSP_ERR_UNSUPPORTED.  As in the
+ *     resampler, only the real parts of the taps are used.
+ *   - The first call on a device (device current) looks up that array's
+ *     address; make it before any stream capture begins.
+ *   - coeffs may be a host or a device pointer; it is copied in stream
+ *     order, so pinned or device taps must stay unchanged until the stream
+ *     reaches the call.
+ *   - The array is shared by every call on the device and keeps the last
+ *     call's taps: calls that overlap in time (different streams or host
+ *     threads without ordering) race on it.  Serialise them.
+ *   - d_in and d_out are device buffers; out_cap < the output count returns
+ *     FDSP_ERR_CAPACITY.  Enqueues on `stream` and returns.
+ * ---------------------------------------------------------------------- */
+#define FDSP_RESAMPLE_STATIC_MAX_COEFFS 8192u
+
+int fdsp_resample_static(uint32_t up_rate, uint32_t down_rate, const fdsp_cf32 *coeffs, uint32_t num_coeffs,
+                         const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *d_out, uint64_t out_cap, uint64_t *n_out,
+                         fdsp_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * NCO frequency shift, one or many channels over one input.
  * Replaces falcon_dsp_freq_shift_cuda (hdr/transform/falcon_dsp_freq_shift_cuda.h:187-212,
  * src/transform/falcon_dsp_freq_shift_cuda.cu:275-488) and the CPU class

@@ -33,7 +33,7 @@ from ._capi import FdspError, cf32, channel_cfg
 __all__ = [
     "FdspError", "FreqShiftCuda", "PolyphaseResamplerCuda", "MultiRateChannelizerCuda", "FirFilterCuda",
     "PolarDiscriminatorCuda", "freq_shift_params", "rat_approx", "freq_shift_cuda", "resample_cuda",
-    "upfirdn_cuda", "fir_filter_cuda", "polar_discriminator_cuda", "channel",
+    "upfirdn_cuda", "fir_filter_cuda", "polar_discriminator_cuda", "channel", "resample_static",
 ]
 
 
@@ -373,6 +373,29 @@ class PolarDiscriminatorCuda(_Handle):
 def freq_shift_cuda(input_sample_rate: int, x, shift):
     """freq_shift_cuda (src/transform/falcon_dsp_freq_shift_cuda.cu:90-119)."""
     return FreqShiftCuda(input_sample_rate, shift).apply(x)
+
+
+RESAMPLE_STATIC_MAX_COEFFS = 8192
+
+
+def resample_static(up_rate: int, down_rate: int, coeffs, x, out):
+    """One-shot resampling of a CUDA complex64 tensor through
+    fdsp_resample_static, the entry point that allocates nothing: the taps go
+    into a fixed 64 KiB device array (at most RESAMPLE_STATIC_MAX_COEFFS
+    taps) and ``out`` must be a preallocated CUDA complex64 tensor.  Equal to
+    a fresh PolyphaseResamplerCuda(up_rate, down_rate, coeffs).apply(x).
+    Calls that overlap in time share that array and race on it."""
+    if not (_is_tensor(x) and _is_tensor(out)):
+        raise TypeError("resample_static takes CUDA tensors for x and out")
+    taps = _c64(coeffs)
+    if taps.size > RESAMPLE_STATIC_MAX_COEFFS:
+        raise ValueError(f"resample_static: {taps.size} taps exceed the fixed array of "
+                         f"{RESAMPLE_STATIC_MAX_COEFFS}")
+    x = _dev_c64(x)
+    got = C.c_uint64()
+    _capi.call("fdsp_resample_static", int(up_rate), int(down_rate), _ptr(taps), taps.size, _tptr(x), x.numel(),
+               _tptr(out), out.numel(), C.byref(got), C.c_void_p(_stream_handle()))
+    return out[: got.value]
 
 
 def resample_cuda(input_sample_rate: int, x, coeffs, output_sample_rate: int):

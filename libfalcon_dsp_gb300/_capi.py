@@ -80,6 +80,7 @@ SIGNATURES = {
     "fdsp_resampler_state": [_vp, _pu32, _pu64],
     "fdsp_resampler_apply": [_vp, _vp, _u64, _vp, _u64, _pu64, _vp],
     "fdsp_resampler_apply_host": [_vp, _vp, _u64, _vp, _u64, _pu64, _vp],
+    "fdsp_resample_static": [_u32, _u32, _vp, _u32, _vp, _u64, _vp, _u64, _pu64, _vp],
     "fdsp_freq_shift_create": [_u32, C.POINTER(_i32), _u32, _pp],
     "fdsp_freq_shift_destroy": [_vp],
     "fdsp_freq_shift_reset": [_vp],
