@@ -105,8 +105,8 @@ typedef struct fdsp_channelizer fdsp_channelizer;
 /* Arithmetic of the channelizer's filter-bank contraction. */
 enum fdsp_precision {
     FDSP_PRECISION_FP32 = 0,     /* plain FP32 complex arithmetic on the SIMT cores (default) */
-    FDSP_PRECISION_FP16X3 = 1,   /* tensor cores: FP16 hi+lo split of data and taps, 3 products, FP32 accumulate */
-    FDSP_PRECISION_BF16X3 = 2    /* tensor cores: BF16 hi+lo split, 3 products, FP32 accumulate */
+    FDSP_PRECISION_FP16X3 = 1,   /* tensor cores: FP16 hi+lo split of data and taps, (hi+lo)(hi+lo), FP32 accumulate */
+    FDSP_PRECISION_BF16X3 = 2    /* tensor cores: BF16 hi+lo split, (hi+lo)(hi+lo), FP32 accumulate */
 };
 
 /* initialize(input_sample_rate, channels)
@@ -128,6 +128,11 @@ int fdsp_channelizer_apply(fdsp_channelizer *h, const fdsp_cf32 *d_in, uint64_t 
 int fdsp_channelizer_set_precision(fdsp_channelizer *h, int precision);
 /* Kernel launches the most recent apply enqueued (diagnostics, profiling). */
 int fdsp_channelizer_kernel_launches(const fdsp_channelizer *h, uint32_t *n);
+/* Decimation groups that the most recent apply computed on the tensor-core
+ * kernel; the rest of the groups took the FP32 kernel (configurations outside
+ * the tensor-core kernel's limits, or precision FP32).  No counterpart in the
+ * reference, which has one arithmetic path. */
+int fdsp_channelizer_tc_groups(const fdsp_channelizer *h, uint32_t *n);
 /* apply(in, out) on host buffers (copies in, computes, copies out, syncs). */
 int fdsp_channelizer_apply_host(fdsp_channelizer *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,
                                 const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);

@@ -151,12 +151,19 @@ class MultiRateChannelizerCuda(_Handle):
 
     def set_precision(self, mode: str = "fp32") -> None:
         """'fp32' (SIMT FP32, default), or the tensor-core split-precision forms
-        'fp16x3' / 'bf16x3' (hi+lo operands, 3 products, FP32 accumulation)."""
+        'fp16x3' / 'bf16x3' (hi+lo operands, full (hi+lo)(hi+lo) product,
+        FP32 accumulation)."""
         _capi.call("fdsp_channelizer_set_precision", self._h, self.PRECISION[mode])
 
     def kernel_launches(self) -> int:
         v = C.c_uint32()
         _capi.call("fdsp_channelizer_kernel_launches", self._h, C.byref(v))
+        return v.value
+
+    def tc_groups(self) -> int:
+        """Decimation groups the last apply computed on the tensor-core kernel."""
+        v = C.c_uint32()
+        _capi.call("fdsp_channelizer_tc_groups", self._h, C.byref(v))
         return v.value
 
     def reset_state(self) -> None:

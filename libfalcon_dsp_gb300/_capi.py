@@ -70,6 +70,7 @@ SIGNATURES = {
     "fdsp_channelizer_apply": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
     "fdsp_channelizer_apply_host": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
     "fdsp_channelizer_kernel_launches": [_vp, _pu32],
+    "fdsp_channelizer_tc_groups": [_vp, _pu32],
     "fdsp_channelizer_set_precision": [_vp, C.c_int],
     "fdsp_resampler_create": [_u32, _u32, _vp, _u32, _pp],
     "fdsp_resampler_destroy": [_vp],

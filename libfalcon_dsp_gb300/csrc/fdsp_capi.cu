@@ -240,6 +240,13 @@ int fdsp_channelizer_kernel_launches(const fdsp_channelizer* h, uint32_t* n) {
   return FDSP_OK;
 }
 
+int fdsp_channelizer_tc_groups(const fdsp_channelizer* h, uint32_t* n) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!n) return FDSP_ERR_INVALID_ARG;
+  *n = (uint32_t)h->eng.tc_groups_last();
+  return FDSP_OK;
+}
+
 int fdsp_channelizer_apply_host(fdsp_channelizer* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* const* h_out,
                                 const uint64_t* out_cap, uint64_t* n_out, fdsp_stream_t stream) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;

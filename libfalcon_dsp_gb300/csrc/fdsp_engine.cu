@@ -660,6 +660,7 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
 int PolyEngine::apply(const float2* d_in, uint64_t n, float2* const* out, const uint64_t* cap, uint64_t* n_out,
                       cudaStream_t stream) {
   launches_last_ = 0;
+  tc_groups_last_ = 0;
   if (n > 0 && d_in == nullptr) return FDSP_ERR_INVALID_ARG;
   if (n >= (1ull << 31)) return FDSP_ERR_UNSUPPORTED;
   for (auto& k : classes_) k.M = class_out_count(k, n);

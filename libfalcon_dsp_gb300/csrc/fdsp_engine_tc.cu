@@ -1,31 +1,46 @@
 // Tensor-core form of the polyphase engine (tcgen05, sm_103a).
 //
 // The fused shift + polyphase contraction of one decimation group is recast
-// as a dense matrix product per (tap chunk, output class r):
+// as dense matrix products over 128-row tiles:
 //
 //     Y[j][c] = sum_k X[j][k] * G[k][c]
 //
-//   j  output row (window end delta_r + j*D),           M = 128 rows per CTA
-//   k  tap index of the padded window (T_pad <= 64),    K = 2*T_pad (re/im)
-//   c  channel of the chunk (<= 64), re and im columns, N = 2*n padded to 16
+//   j  output row of the tile (window end delta + j D),   M = 128
+//   k  tap of the window,                                 K = 8 x taps
+//   c  Re / Im column of each channel,                    N <= 128
 //
-// X rows are the raw (unshifted) input windows, G the NCO-modulated taps of
-// phase phi_r (the same folding as the FP32 engine).  Both are split into
-// hi + lo 16-bit parts and the product is taken as hi*hi + hi*lo + lo*hi with
-// FP32 accumulation in tensor memory, which keeps ~2^-21 relative accuracy
-// (far above the 60 dB SNR target) at tensor-core throughput.
+// X[j][k] is input sample (j D + k + offset): a Hankel matrix over the input
+// de-interleaved by D.  Each sample is held in shared memory as one 16-byte
+// record of its hi and lo 16-bit parts, {hi(re,im), lo(re,im), hi, lo}, so
+// that the K-major core matrix of 8 rows x 16 bytes for rows j..j+7 and tap k
+// is 8 consecutive records of phase (k mod D): the MMA reads every window of
+// the tile straight from the staged input through its descriptor (leading
+// byte offset = one phase array, stride byte offset = 8 records), with no
+// per-row copy.  The matching B record of a tap holds the NCO-modulated tap's
+// hi and lo parts ordered so that the 8 products sum to the full
+// (hi + lo) x (hi + lo) complex product with FP32 accumulation in tensor
+// memory (~2^-22 relative, far above the 60 dB target).
 //
-//   * A (X) lives in TMEM: thread j of the CTA owns TMEM lane j and writes its
-//     window as packed 16-bit (re, im) pairs, one 32-bit column per sample,
-//     with tcgen05.st -- no shared-memory traffic for the large operand.
-//   * B (G) is staged in shared memory in the K-major no-swizzle layout
-//     (8 x 16-byte core matrices), precomputed on the host per phase.
-//   * One thread issues 3 MMAs per K-step of 16 and commits to an mbarrier;
-//     every wait is bounded and reports through an error flag.
-//   * The epilogue loads each row's accumulators (tcgen05.ld), rotates them by
-//     the exact integer NCO phase of the window start, applies the exact FP32
-//     split-sum correction for windows that straddle the NCO rollover, and
-//     stores each channel's output sample.
+// Work sets (class x output phase) of a group whose windows end close
+// together are merged into one product (a merge set): each one's taps sit at
+// its own offset of a common window (zeros elsewhere) and its channels side by
+// side along N, so one MMA chain serves up to 64 channels.  The offsets follow
+// the streaming state, so every CTA assembles the merged B in shared memory at
+// start from per-phase blocks precomputed on the host.
+//
+// Persistent warp-specialised CTA, one per SM (all 512 TMEM columns):
+//   warps 0-2   producers: assemble B and the channel constants once, then
+//               per tile stage the de-interleaved input records (cp.async,
+//               zero-filled outside the data) into one of up to four buffers,
+//               several tiles in flight;
+//   warp 3      MMA issuer: per (tile, merge set) waits for the staged tile
+//               and a drained accumulator slot, issues Kw/2 MMAs, commits;
+//   warps 4-19  epilogue, four groups of four warps (one per TMEM lane
+//               quarter); group g drains items g, g+4, ... (accumulator slot
+//               g): rotates by the exact integer NCO phase of each window
+//               start, fixes windows that straddle the NCO rollover with an
+//               exact FP32 split sum, and stores.
+// Every mbarrier wait is bounded and reports through an error flag.
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 
@@ -40,24 +55,46 @@
 
 namespace fdsp {
 
-constexpr int kTcThreads = 672;         // 4 producer warps + 1 MMA warp + 16 epilogue warps
-constexpr int kTcProdThreads = 128;     // one producer warp per TMEM lane quarter
-constexpr int kTcEpiThreads = 512;      // four epilogue warps per TMEM lane quarter
-constexpr uint32_t kTmemCols = 512;     // [A slot 0 | A slot 1 | D slot 0 | D slot 1], 128 columns each
+constexpr int kTcThreads = 640;       // 3 producer warps + 1 MMA warp + 16 epilogue warps
+constexpr int kTcProdThreads = 96;    // (20 warps: 5 per SM sub-partition, up to 96 registers each)
+constexpr int kTcDSlots = 4;          // accumulator slots = epilogue groups (items in flight)
+constexpr uint32_t kTcDCols = 128;    // accumulator columns per slot (N <= 128)
+constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kWaitPolls = 1u << 20;
+constexpr int kTcChunk = 32;          // channels per chunk (64 columns)
+constexpr int kTcMaxTaps = 64;        // taps per phase of a chunk
+constexpr int kTcMaxKw = 128;         // taps of a merged window
+constexpr size_t kTcSmemMax = 225 * 1024;
+constexpr int kTcMaxBuf = 4;          // input buffers
 
-using TcMeta = OutMeta;
+// Constants of one channel slot (Re/Im column pair) of a merge set, staged
+// in shared memory.  The first 48 bytes are read for every output (three
+// 16-byte loads); the rest only once per item and on the exact path.
+struct SlotMeta {
+  uint32_t om_lo, om_hi;  // NCO turns per sample (2^-64 units; 0: no shift)
+  float2* out;            // output base of the channel
+  uint32_t R;             // counter rollover (0x7fffffff: no shift or general)
+  uint32_t Tm1;           // taps - 1 (0x7fffffff: general, every output exact)
+  int32_t U, r;           // output m = r + U j
+  int32_t J;              // rows with an output (0: padding slot)
+  uint32_t short_r;       // 1: R <= 127 D + T, the row counter is reduced in full
+  uint64_t fastmod;       // ceil(2^64 / R)
+  int32_t delta;          // window end of row 0
+  int32_t T;
+  OutMeta nco;            // full NCO constants (row-0 counter, exact path)
+  const float2* taps32;   // FP32 modulated taps [T][tstride] of the work set
+  int32_t tstride, tidx;
+  int32_t pad_[2];
+};
+static_assert(sizeof(SlotMeta) == 128, "slot constants layout");
 
-__device__ __forceinline__ float2 cmul_tc(float2 a, float2 b) {
-  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
-}
-
-__device__ __forceinline__ float2 phasor64_tc(uint64_t turns64) {
-  const int32_t top = (int32_t)(turns64 >> 32);
-  const float a = (float)top * 1.4629180792671596e-09f;  // 2 pi / 2^32
-  float s, c;
-  __sincosf(a, &s, &c);
-  return make_float2(c, s);
+// Shared-memory load of read-only slot constants: plain (non-volatile) asm
+// without a memory clobber, so the compiler may hoist it above the output
+// stores of earlier slots (they cannot alias).
+__device__ __forceinline__ uint4 lds_u4(uint32_t a) {
+  uint4 v;
+  asm("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
+  return v;
 }
 
 __device__ __forceinline__ float2 load_x(const TcLaunch& L, int64_t v) {
@@ -85,47 +122,6 @@ __device__ __forceinline__ void split2(float2 x, uint32_t& hi, uint32_t& lo) {
   }
 }
 
-// Item sequence of one persistent CTA, tile-major: tiles blockIdx.x,
-// blockIdx.x + gridDim.x, ... and within a tile every work set of the group
-// that has rows there.  Producers and the epilogue walk it independently.
-struct ItemIter {
-  int tile, wi;
-};
-
-__device__ __forceinline__ void item_settle(const TcLaunch& L, const TcGroup& G, ItemIter& t) {
-  while (t.tile < G.ntiles) {
-    while (t.wi < G.ws_end && t.tile >= L.ws[t.wi].ntiles) ++t.wi;
-    if (t.wi < G.ws_end) return;
-    t.tile += gridDim.x;
-    t.wi = G.ws_begin;
-  }
-}
-__device__ __forceinline__ ItemIter item_first(const TcLaunch& L, const TcGroup& G) {
-  ItemIter t{(int)blockIdx.x, G.ws_begin};
-  item_settle(L, G, t);
-  return t;
-}
-__device__ __forceinline__ ItemIter item_next(const TcLaunch& L, const TcGroup& G, ItemIter t) {
-  ++t.wi;
-  item_settle(L, G, t);
-  return t;
-}
-
-// Asynchronous 8-byte copy of pre-split input sample v (block relative,
-// v >= -H; {hi, lo} packed 16-bit pairs; zero-fill outside the data) into
-// shared memory.
-__device__ __forceinline__ void stage_sample(const TcLaunch& L, int64_t v, uint2* dst) {
-  const int64_t u = v + L.H;
-  const uint2* src = L.xhl;
-  uint32_t bytes = 0;
-  if (u >= 0 && u < L.N + L.H) {
-    src = L.xhl + u;
-    bytes = 8;
-  }
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(bytes)
-               : "memory");
-}
-
 // [history | block] -> packed {hi, lo} 16-bit pairs, once per apply: every
 // sample is used by many windows, so the split is not repeated per use.
 template <int FMT>
@@ -140,46 +136,63 @@ __global__ void split_input_kernel(const float2* __restrict__ block, const float
   }
 }
 
-// Persistent warp-specialised CTA (one per SM, all 512 TMEM columns):
-//   warps 0-3   producers (TMEM lane quarter = warp): stage the B operands of
-//               every work set once, then per tile stage the input (kDeint:
-//               the whole tile de-interleaved by D in a double buffer, shared
-//               by all work sets; otherwise each thread prefetches its own
-//               row's window one item ahead) and build A for each work set into
-//               one of two TMEM A slots;
-//   warp 4      MMA issuer: waits for a built A slot and a drained accumulator
-//               slot, issues the 3 x (T/8) MMAs, commits;
-//   warps 5-20  epilogue (four warps per lane quarter, splitting the channels):
-//               drain an accumulator slot (tcgen05.ld), rotate, fix rollover
-//               straddles, store, release the slot.
-// Shared memory: [B hi|lo of every work set][channel constants][input].
-template <int FMT, bool kDeint>
-__global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_constant__ TcLaunch L, int g) {
+// Asynchronous copy of input sample v (block relative), its 8-byte
+// pre-split {hi, lo} pair, into one half of a 16-byte record (zero outside
+// the data).  Two lanes fill the two halves of a record, so a warp writes 256
+// contiguous bytes of shared memory per instruction.
+__device__ __forceinline__ void stage_half(const TcLaunch& L, int64_t v, uint32_t dst) {
+  const int64_t u = v + L.H;
+  const uint2* src = L.xhl;
+  uint32_t bytes = 0;
+  if (u >= 0 && u < L.N + L.H) {
+    src = L.xhl + u;
+    bytes = 8;
+  }
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
+__device__ __forceinline__ void mma_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "setp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+      "}\n" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_constant__ TcLaunch L) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ uint32_t tmem_base_s;
-  __shared__ __align__(8) uint64_t bar_a_full[2];    // A slot built                  (128 producer arrivals)
-  __shared__ __align__(8) uint64_t bar_a_empty[2];   // MMA done reading A slot       (commit)
-  __shared__ __align__(8) uint64_t bar_d_full[2];    // accumulator slot ready        (commit)
-  __shared__ __align__(8) uint64_t bar_d_empty[2];   // epilogue drained accumulator  (512 arrivals)
-  __shared__ __align__(8) uint64_t bar_b_full;       // B operands + constants staged (128 arrivals)
+  __shared__ __align__(8) uint64_t bar_in_full[kTcMaxBuf];   // tile staged        (one arrival per producer warp)
+  __shared__ __align__(8) uint64_t bar_in_empty[kTcMaxBuf];  // tile's MMAs done   (commit)
+  __shared__ __align__(8) uint64_t bar_d_full[kTcDSlots];    // accumulator ready  (commit)
+  __shared__ __align__(8) uint64_t bar_d_empty[kTcDSlots];   // accumulator drained (one arrival per group warp)
+  __shared__ __align__(8) uint64_t bar_b_full;               // B + slot constants (one arrival per producer warp)
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
-  const TcGroup& G = L.groups[g];
-  const int D = G.D;
-  uint2* xin = reinterpret_cast<uint2*>(smem + G.in_off);
+  const int lane_id = tid & 31;
+  const int D = L.D;
+  const int nms = L.nmsets;
 
   if (warp == 0) {
     tc::tmem_alloc(&tmem_base_s, kTmemCols);
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&bar_a_full[i], kTcProdThreads);
-      tc::mbar_init(&bar_a_empty[i], 1);
-      tc::mbar_init(&bar_d_full[i], 1);
-      tc::mbar_init(&bar_d_empty[i], kTcEpiThreads);
+    for (int i = 0; i < kTcMaxBuf; ++i) {
+      tc::mbar_init(&bar_in_full[i], kTcProdThreads / 32);
+      tc::mbar_init(&bar_in_empty[i], 1);
     }
-    tc::mbar_init(&bar_b_full, kTcProdThreads);
+    for (int i = 0; i < kTcDSlots; ++i) {
+      tc::mbar_init(&bar_d_full[i], 1);
+      tc::mbar_init(&bar_d_empty[i], 4);
+    }
+    tc::mbar_init(&bar_b_full, kTcProdThreads / 32);
     tc::mbar_fence_init();
   }
   tc::fence_before_sync();
@@ -188,277 +201,353 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
   const uint32_t tbase = tmem_base_s;
   bool failed = false;
 
-  if (warp < 4) {
+  if (warp < 3) {
     // ------------------------------------------------------------ producers
-    // Every decision to stop is taken jointly (bar.red.or over the 128
-    // producer threads) so no producer is ever left alone at a barrier.
-    const uint32_t lane = (uint32_t)(warp * 32) << 16;
-    const int row = tid;  // 0..127 = TMEM lane
-    for (int wi = G.ws_begin; wi < G.ws_end; ++wi) {
-      const TcWorkSet& W = L.ws[wi];
-      uint8_t* bhi_s = smem + W.boff;
-      for (int i = tid; i < W.bbytes / 16; i += kTcProdThreads) {
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(tc::smem_u32(bhi_s + 16 * i)),
-                     "l"(W.bhi + 16 * i)
-                     : "memory");
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(tc::smem_u32(bhi_s + W.bbytes + 16 * i)),
-                     "l"(W.blo + 16 * i)
-                     : "memory");
+    // B of every merge set: core (cg, k) comes from the work set that owns
+    // column group cg and tap k, else it is zero.
+    for (int mi = 0; mi < nms; ++mi) {
+      const TcMset& M = L.ms[mi];
+      const int ncores = (M.N / 8) * M.Kw;
+      for (int p = tid; p < ncores * 8; p += kTcProdThreads) {
+        const int core = p >> 3, piece = p & 7;
+        const int cg = core / M.Kw, k = core - cg * M.Kw;
+        uint8_t* dst = smem + M.boff + (size_t)core * 128 + piece * 16;
+        const uint8_t* src = nullptr;
+        for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
+          const TcWorkSet& W = L.ws[wi];
+          if (cg >= W.cg0 && cg < W.cg0 + W.ng && k >= W.o && k < W.o + W.T) {
+            src = W.b + ((size_t)(cg - W.cg0) * W.T + (k - W.o)) * 128 + piece * 16;
+            break;
+          }
+        }
+        if (src)
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
+        else
+          *reinterpret_cast<uint4*>(dst) = make_uint4(0u, 0u, 0u, 0u);
       }
-      if (tid < W.n) {
-        const int c = W.ch[tid];
-        const NcoConst nc = L.nco[c];
-        OutMeta m;
-        m.omega64 = nc.omega64;
-        m.wrap64 = nc.wrap64;
-        m.fastmod = nc.fastmod;
-        m.out = L.out[c];
-        m.rollover = nc.rollover;
-        m.base = L.nco_base[c];
-        m.enabled = nc.enabled;
-        m.pad_ = 0;
-        reinterpret_cast<OutMeta*>(smem + W.moff)[tid] = m;
+      // channel slot s = columns 2s, 2s+1
+      for (int s = tid; s < M.N / 2; s += kTcProdThreads) {
+        SlotMeta sm;
+        std::memset(&sm, 0, sizeof(sm));
+        sm.R = 0x7fffffffu;
+        for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
+          const TcWorkSet& W = L.ws[wi];
+          const int i = s - 4 * W.cg0;
+          if (i >= 0 && i < 4 * W.ng) {
+            if (i < W.n) {
+              const int c = W.ch[i];
+              const NcoConst nc = L.nco[c];
+              sm.nco.omega64 = nc.omega64;
+              sm.nco.wrap64 = nc.wrap64;
+              sm.nco.fastmod = nc.fastmod;
+              sm.nco.out = L.out[c];
+              sm.nco.rollover = nc.rollover;
+              sm.nco.base = L.nco_base[c];
+              sm.nco.enabled = nc.enabled;
+              // fast path: R < 2^31 (row counters in 32 bits); the counter
+              // of row `row` is row 0's plus row D, past the rollover at most
+              // once when 127 D + T < R, else reduced with the fast modulo;
+              // R >= 2^31 ("general") takes the exact path for every output
+              const bool general = nc.enabled && nc.rollover >= 0x80000000u;
+              sm.short_r =
+                  (nc.enabled && !general && (uint64_t)nc.rollover <= 127ull * D + (uint64_t)W.T) ? 1u : 0u;
+              sm.fastmod = nc.fastmod;
+              sm.om_lo = nc.enabled && !general ? (uint32_t)nc.omega64 : 0u;
+              sm.om_hi = nc.enabled && !general ? (uint32_t)(nc.omega64 >> 32) : 0u;
+              sm.out = L.out[c];
+              sm.R = nc.enabled && !general ? nc.rollover : 0x7fffffffu;
+              sm.taps32 = W.taps32;
+              sm.delta = W.delta;
+              sm.T = W.T;
+              sm.Tm1 = general ? 0x7fffffffu : (uint32_t)(W.T - 1);
+              sm.U = W.U;
+              sm.r = W.r;
+              sm.J = W.J;
+              sm.tstride = W.n;
+              sm.tidx = i;
+            }
+            break;
+          }
+        }
+        reinterpret_cast<SlotMeta*>(smem + M.moff)[s] = sm;
       }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     tc::fence_proxy_async_smem();
-    tc::mbar_arrive(&bar_b_full);
+    __syncwarp();
+    if (lane_id == 0) tc::mbar_arrive(&bar_b_full);
 
-    ItemIter itr = item_first(L, G);
-    int it = 0;
-    int cur_tile = -1;
-    int tile_ord = 0;            // tiles begun by this CTA (tile buffer = tile_ord & 1)
-    const int wp = G.win_pitch;  // window mode: uint2 per staged row
-    auto stage_tile = [&](int tile, int buf) {
-      const int64_t sb = (int64_t)tile * 128 * D + G.delta_min - G.tmax + 1;
-      const int len = 127 * D + G.delta_span + G.tmax;
-      uint2* dst = xin + buf * G.tile_elems;
-      for (int t = tid; t < len; t += kTcProdThreads) {
-        const int q = t / D;
-        stage_sample(L, sb + t, dst + (t - q * D) * G.P + q);
-      }
-    };
-    auto stage_window = [&](const ItemIter& t, int buf) {
-      const TcWorkSet& WT = L.ws[t.wi];
-      const int64_t w0 = (int64_t)WT.delta + ((int64_t)t.tile * 128 + row) * D - WT.T + 1;
-      uint2* dst = xin + (buf * 128 + row) * wp;
-      for (int k = 0; k < WT.T; ++k) stage_sample(L, w0 + k, dst + k);
-    };
-    if (itr.tile < G.ntiles) {
-      if constexpr (kDeint)
-        stage_tile(itr.tile, 0);
-      else
-        stage_window(itr, 0);
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-
-    while (itr.tile < G.ntiles) {
-      const TcWorkSet& W = L.ws[itr.wi];
-      const int T = W.T;
-      const ItemIter nx = item_next(L, G, itr);
-      if constexpr (kDeint) {
-        if (itr.tile != cur_tile) {
-          // this tile's copies (issued one tile ago) complete, then a producer
-          // barrier: every copy is visible and every producer has finished
-          // reading the previous tile, whose buffer now takes the prefetch of
-          // this CTA's next tile
-          asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-          tc::named_bar_sync(1, kTcProdThreads);
-          const int nt = itr.tile + (int)gridDim.x;
-          if (nt < G.ntiles) stage_tile(nt, (tile_ord + 1) & 1);
-          asm volatile("cp.async.commit_group;\n" ::: "memory");
-          cur_tile = itr.tile;
-          ++tile_ord;
+    // tiles: record (v, q) of tile t = input sample 128 t D + B0 + q D + v.
+    // Up to nbuf - 1 tiles' copies stay in flight; the oldest is announced
+    // once its copy group is complete, before the next tile's copies are
+    // issued (the buffer of tile t is reused for tile t + nbuf after the
+    // MMAs of tile t are done).
+    const int nbuf = L.nbuf;
+    const int lag = nbuf - 1;
+    int tile_ord = 0;
+    int announced = 0;
+    // staging map: lanes 2i, 2i+1 write the two halves of record (v, q),
+    // records of one phase in consecutive lanes (q fastest)
+    const int V = L.V;
+    const uint32_t half = (uint32_t)(tid & 1) * 8u;
+    const int rsub = tid >> 1;  // 0..47
+    for (int tile = blockIdx.x; tile < L.ntiles; tile += gridDim.x, ++tile_ord) {
+      const int buf = tile_ord % nbuf;
+      if (tile_ord >= lag && lag > 0) {
+        switch (lag) {  // all but the lag - 1 most recent groups
+          case 1: asm volatile("cp.async.wait_group 0;\n" ::: "memory"); break;
+          case 2: asm volatile("cp.async.wait_group 1;\n" ::: "memory"); break;
+          default: asm volatile("cp.async.wait_group 2;\n" ::: "memory"); break;
         }
-      } else {
-        // prefetch the next item's window (own row), then wait for this item's
-        if (nx.tile < G.ntiles) stage_window(nx, (it + 1) & 1);
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[announced % nbuf]);
+        ++announced;
       }
-      const uint32_t slot = (uint32_t)(it & 1);
-      // A slot free once the MMAs of item it-2 are done
-      bool ok = true;
-      if (it >= 2) ok = tc::mbar_wait_bounded(&bar_a_empty[slot], (uint32_t)(((it - 2) >> 1) & 1), kWaitPolls);
-      if (tc::named_bar_red_or(2, kTcProdThreads, !ok || failed)) {
-        failed = true;
-        break;
-      }
-      // build A from shared memory: this row's window, hi and lo parts
-      const uint32_t acol = slot * 128u;
-      if constexpr (kDeint) {
-        const int a0 = (W.delta - G.delta_min) + (G.tmax - T);
-        const uint2* xt = xin + ((tile_ord - 1) & 1) * G.tile_elems;
-        int q0 = a0 / D;
-        int b0 = a0 - q0 * D;
-        const uint2* xp = xt + b0 * G.P + q0 + row;
-        const int wrap = 1 - D * G.P;
-        for (int kc = 0; kc < T; kc += 8) {
-          uint32_t hi[8], lo[8];
-#pragma unroll
-          for (int e = 0; e < 8; ++e) {
-            const uint2 hl = *xp;
-            hi[e] = hl.x;
-            lo[e] = hl.y;
-            xp += G.P;
-            if (++b0 == D) {
-              b0 = 0;
-              xp += wrap;
-            }
-          }
-          tc::tmem_st8(tbase + lane + acol + kc, hi);
-          tc::tmem_st8(tbase + lane + acol + 64 + kc, lo);
-        }
-      } else {
-        const uint2* xr = xin + ((it & 1) * 128 + row) * wp;
-        for (int kc = 0; kc < T; kc += 8) {
-          uint32_t hi[8], lo[8];
-#pragma unroll
-          for (int e = 0; e < 8; ++e) {
-            const uint2 hl = xr[kc + e];
-            hi[e] = hl.x;
-            lo[e] = hl.y;
-          }
-          tc::tmem_st8(tbase + lane + acol + kc, hi);
-          tc::tmem_st8(tbase + lane + acol + 64 + kc, lo);
+      if (tile_ord >= nbuf) {
+        const int use = tile_ord / nbuf - 1;  // earlier use of this buffer
+        const bool ok = tc::mbar_wait_bounded(&bar_in_empty[buf], (uint32_t)(use & 1), kWaitPolls);
+        if (__any_sync(0xffffffffu, !ok)) {
+          failed = true;
+          break;
         }
       }
-      tc::tmem_wait_st();
-      tc::fence_before_sync();
-      tc::mbar_arrive(&bar_a_full[slot]);
-      itr = nx;
-      ++it;
+      const uint32_t xb = tc::smem_u32(smem + L.in_off + buf * L.in_bytes);
+      const int64_t tb = (int64_t)tile * 128 * D + L.B0;
+      for (int v = 0; v < V; ++v)
+        for (int q = rsub; q < L.Qp; q += kTcProdThreads / 2)
+          stage_half(L, tb + (int64_t)q * D + v, xb + (uint32_t)(v * L.Qp + q) * 16u + half);
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      if (lag == 0) {
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[0]);
+        ++announced;
+      }
     }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    if (failed && tid == 0) atomicExch(L.err, 1);
-  } else if (warp == 4) {
+    if (!failed) {
+      tc::fence_proxy_async_smem();
+      __syncwarp();
+      for (; announced < tile_ord; ++announced)
+        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[announced % nbuf]);
+    }
+    if (failed && lane_id == 0) atomicExch(L.err, 1);
+  } else if (warp == 3) {
     // ------------------------------------------------------------ MMA issuer
+    // A-offset table of every merge set: entry kp = record index (v Qp + q)
+    // of taps 2kp, 2kp+1 in a staged tile, i.e. the A descriptor's address
+    // field relative to the buffer (computed once, by all 32 lanes)
+    uint32_t* tab = reinterpret_cast<uint32_t*>(smem + L.tab_off);
+    for (int mi = 0; mi < nms; ++mi) {
+      const TcMset& M = L.ms[mi];
+      const int nkp = M.Kw / 2;
+      for (int kp = lane_id; kp < ((nkp + 3) & ~3); kp += 32) {
+        uint32_t e = 0;
+        if (kp < nkp) {
+          const int s = M.a + 2 * kp;
+          const int q = L.wrap ? s / D : 0;
+          e = (uint32_t)((s - q * D) * L.Qp + q);
+        }
+        tab[M.toff + kp] = e;
+      }
+    }
+    __syncwarp();
     bool ok = tc::mbar_wait_bounded(&bar_b_full, 0u, kWaitPolls);
     if (__any_sync(0xffffffffu, !ok)) failed = true;
-    ItemIter itr = item_first(L, G);
     int it = 0;
-    while (!failed && itr.tile < G.ntiles) {
-      const TcWorkSet& W = L.ws[itr.wi];
-      const int T = W.T;
-      const uint32_t slot = (uint32_t)(it & 1);
-      ok = tc::mbar_wait_bounded(&bar_a_full[slot], (uint32_t)((it >> 1) & 1), kWaitPolls);
-      if (ok && it >= 2) ok = tc::mbar_wait_bounded(&bar_d_empty[slot], (uint32_t)(((it - 2) >> 1) & 1), kWaitPolls);
+    int tile_ord = 0;
+    const int nbuf = L.nbuf;
+    // descriptor words: low = address >> 4 | (leading byte offset >> 4) << 16,
+    // high = (stride byte offset >> 4) | version 1 (bit 46)
+    const uint32_t a_hi = (128u >> 4) | (1u << 14);
+    for (int tile = blockIdx.x; !failed && tile < L.ntiles; tile += gridDim.x, ++tile_ord) {
+      const int buf = tile_ord % nbuf;
+      const int use = tile_ord / nbuf;
+      ok = tc::mbar_wait_bounded(&bar_in_full[buf], (uint32_t)(use & 1), kWaitPolls);
       if (__any_sync(0xffffffffu, !ok)) {
         failed = true;
         break;
       }
       tc::fence_after_sync();
-      if ((tid & 31) == 0) {
-        const uint32_t idesc = tc::idesc_f16(FMT, 128, W.N_pad);
-        const uint32_t sbo = 16u * (2u * T);
-        const uint32_t bh = tc::smem_u32(smem + W.boff);
-        const uint32_t bl = bh + W.bbytes;
-        const uint32_t acol = slot * 128u;
-        const uint32_t dcol = 256u + slot * 128u;
-        for (int s2 = 0; s2 < T / 8; ++s2) {
-          const uint64_t dh = tc::smem_desc(bh + 256u * s2, 128u, sbo);
-          const uint64_t dl = tc::smem_desc(bl + 256u * s2, 128u, sbo);
-          tc::mma_ts(tbase + dcol, tbase + acol + 8 * s2, dh, idesc, s2 > 0 ? 1u : 0u);
-          tc::mma_ts(tbase + dcol, tbase + acol + 8 * s2, dl, idesc, 1u);
-          tc::mma_ts(tbase + dcol, tbase + acol + 64 + 8 * s2, dh, idesc, 1u);
+      const uint32_t xb = tc::smem_u32(smem + L.in_off + buf * L.in_bytes);
+      const uint32_t a_lo0 = ((xb >> 4) & 0x3FFFu) | ((((uint32_t)L.Qp * 16u) >> 4) << 16);
+      for (int mi = 0; mi < nms; ++mi, ++it) {
+        const uint32_t ds = (uint32_t)(it % kTcDSlots);
+        if (it >= kTcDSlots) {
+          ok = tc::mbar_wait_bounded(&bar_d_empty[ds], (uint32_t)(((it - kTcDSlots) / kTcDSlots) & 1), kWaitPolls);
+          if (__any_sync(0xffffffffu, !ok)) {
+            failed = true;
+            break;
+          }
+          tc::fence_after_sync();
         }
-        tc::mma_commit(&bar_a_empty[slot]);
-        tc::mma_commit(&bar_d_full[slot]);
+        if (lane_id == 0) {
+          // taps 2kp, 2kp+1 read records (v, q) and (v + 1, q) of the tile
+          // (phase D is phase 0 one row on): A address = buffer + tab[kp];
+          // B advances one 256-byte pair of cores per MMA
+          const TcMset& M = L.ms[mi];
+          const uint32_t idesc = tc::idesc_f16(FMT, 128, (uint32_t)M.N);
+          const uint32_t bb = tc::smem_u32(smem + M.boff);
+          const uint32_t b_lo0 = ((bb >> 4) & 0x3FFFu) | ((128u >> 4) << 16);
+          const uint32_t b_hi = (((uint32_t)M.Kw * 128u) >> 4) | (1u << 14);
+          const uint32_t d_tm = tbase + ds * kTcDCols;
+          const uint4* t4 = reinterpret_cast<const uint4*>(tab + M.toff);
+          const int nkp = M.Kw / 2;
+          for (int kp = 0; kp < nkp; kp += 4) {
+            // the four descriptor pairs are ready before the first MMA issues
+            const uint4 o = t4[kp >> 2];
+            const uint32_t bl = b_lo0 + (uint32_t)kp * 16u;
+            const uint64_t da0 = ((uint64_t)a_hi << 32) | (a_lo0 + o.x);
+            const uint64_t da1 = ((uint64_t)a_hi << 32) | (a_lo0 + o.y);
+            const uint64_t da2 = ((uint64_t)a_hi << 32) | (a_lo0 + o.z);
+            const uint64_t da3 = ((uint64_t)a_hi << 32) | (a_lo0 + o.w);
+            const uint64_t db0 = ((uint64_t)b_hi << 32) | bl;
+            const uint64_t db1 = ((uint64_t)b_hi << 32) | (bl + 16u);
+            const uint64_t db2 = ((uint64_t)b_hi << 32) | (bl + 32u);
+            const uint64_t db3 = ((uint64_t)b_hi << 32) | (bl + 48u);
+            mma_ss(d_tm, da0, db0, idesc, kp > 0 ? 1u : 0u);
+            if (kp + 1 < nkp) mma_ss(d_tm, da1, db1, idesc, 1u);
+            if (kp + 2 < nkp) mma_ss(d_tm, da2, db2, idesc, 1u);
+            if (kp + 3 < nkp) mma_ss(d_tm, da3, db3, idesc, 1u);
+          }
+          tc::mma_commit(&bar_d_full[ds]);
+        }
+        __syncwarp();
       }
+      if (failed) break;
+      if (lane_id == 0) tc::mma_commit(&bar_in_empty[buf]);
       __syncwarp();
-      itr = item_next(L, G, itr);
-      ++it;
     }
-    if (failed && (tid & 31) == 0) atomicExch(L.err, 1);
+    if (failed && lane_id == 0) atomicExch(L.err, 1);
   } else {
     // ------------------------------------------------------------ epilogue
-    const int ew = warp - 5;                 // 0..15
-    const int quarter = warp & 3;            // TMEM lanes this warp may access
-    const int part = ew >> 2;                // which quarter of the channels
+    // Group eg drains items eg, eg+4, ... (item = tile_ord * nmsets + merge
+    // set; accumulator slot eg); warp w covers TMEM lanes 32 (w % 4) .. +31
+    // for every channel slot.  Each warp runs on its own (no barrier among
+    // epilogue warps), so a stop decision only has to be uniform over it.
+    const int eg = (warp - 4) >> 2;
+    const int quarter = warp & 3;
     const uint32_t lane = (uint32_t)(quarter * 32) << 16;
-    const int row = quarter * 32 + (tid & 31);
-    // stop decisions are uniform over all epilogue threads (bar.red.or)
+    const int row = quarter * 32 + lane_id;
     bool ok = tc::mbar_wait_bounded(&bar_b_full, 0u, kWaitPolls);
-    if (tc::named_bar_red_or(4, kTcEpiThreads, !ok)) failed = true;
-    ItemIter itr = item_first(L, G);
-    int it = 0;
-    while (!failed && itr.tile < G.ntiles) {
-      const TcWorkSet& W = L.ws[itr.wi];
-      const uint32_t slot = (uint32_t)(it & 1);
-      ok = tc::mbar_wait_bounded(&bar_d_full[slot], (uint32_t)((it >> 1) & 1), kWaitPolls);
-      if (tc::named_bar_red_or(4, kTcEpiThreads, !ok)) {
+    if (__any_sync(0xffffffffu, !ok)) failed = true;
+    for (int it = eg; !failed; it += kTcDSlots) {
+      const int tile_ord = it / nms;
+      const int mi = it - tile_ord * nms;
+      const int tile = blockIdx.x + tile_ord * gridDim.x;
+      if (tile >= L.ntiles) break;
+      ok = tc::mbar_wait_bounded(&bar_d_full[eg], (uint32_t)((it / kTcDSlots) & 1), kWaitPolls);
+      if (__any_sync(0xffffffffu, !ok)) {
         failed = true;
         break;
       }
       tc::fence_after_sync();
-      const OutMeta* meta = reinterpret_cast<const OutMeta*>(smem + W.moff);
-      const int T = W.T;
-      const int64_t j = (int64_t)itr.tile * 128 + row;
-      const int64_t w0 = (int64_t)W.delta + j * D - T + 1;
-      const bool row_ok = j < W.J;
-      const int64_t m = (int64_t)W.r + (int64_t)W.U * j;
-      const uint32_t dcol = 256u + slot * 128u;
-      // the four warps of a lane quarter split the channels in 8-channel
-      // chunks: this warp takes chunks [c_lo, c_hi) (at most 2 for n <= 64)
-      const int nch = (W.n + 7) >> 3;
-      const int c_lo = (nch * part) >> 2, c_hi = (nch * (part + 1)) >> 2;
-      const int n_lo = c_lo * 8, n_hi = min(W.n, c_hi * 8);
-      uint32_t vv[2][16];
+      const TcMset& M = L.ms[mi];
+      const SlotMeta* meta = reinterpret_cast<const SlotMeta*>(smem + M.moff);
+      const uint32_t meta_s = tc::smem_u32(smem + M.moff);
+      const int nslots = M.N >> 1;
+      const int64_t j0 = (int64_t)tile * 128;
+      const int64_t j = j0 + row;
+      // row-0 NCO counter of the item for slots lane_id and lane_id + 32:
+      // P0 = (samples since reset at the window start of row 0) mod R; row
+      // `row` then starts at (P0 + row D) mod R: one subtraction unless the
+      // rollover is shorter than the tile
+      uint32_t p0a = 0, p0b = 0;
 #pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        const int cc = c_lo + q;
-        if (cc < c_hi) tc::tmem_ld16(tbase + lane + dcol + 16 * cc, vv[q]);
+      for (int h = 0; h < 2; ++h) {
+        const int si = lane_id + 32 * h;
+        if (si < nslots) {
+          const SlotMeta& sm = meta[si];
+          if (sm.om_lo | sm.om_hi) {
+            // x < R + 2^31 < 2^32 on the fast path; x >= -(T - 1) > -R
+            const int64_t x = (int64_t)sm.nco.base + sm.delta - sm.T + 1 + j0 * D;
+            const uint32_t pr0 = x < 0 ? (uint32_t)(x + sm.R)
+                                       : (uint32_t)__umul64hi(sm.nco.fastmod * (uint64_t)x, (uint64_t)sm.R);
+            if (h == 0) p0a = pr0; else p0b = pr0;
+          }
+        }
       }
-      tc::tmem_wait_ld();
-      // the accumulator slot is free for the next MMAs as soon as it is in
-      // registers
-      tc::fence_before_sync();
-      tc::mbar_arrive(&bar_d_empty[slot]);
-#pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        const int cc = c_lo + q;
-        if (cc >= c_hi) break;
-        const uint32_t* v = vv[q];
-        // 8 channels branch free (so their phase chains interleave); outputs
-        // whose window crosses the NCO rollover are written unrotated and
-        // fixed from that value below (nothing extra stays live)
-        uint32_t slow = 0;
+      const uint32_t rowD = (uint32_t)(row * D);
+      const int32_t j32 = (int32_t)j;
+      const uint32_t dcol = (uint32_t)eg * kTcDCols;
+      const int nch = M.N >> 4;  // 8-slot chunks (16 columns)
+      for (int cc = 0; cc < nch; ++cc) {
+        uint32_t v[16];
+        tc::tmem_ld16(tbase + lane + dcol + 16 * cc, v);
+        tc::tmem_wait_ld();
+        if (cc + 1 == nch) {
+          // the slot is free for the MMAs once every lane holds its last part
+          tc::fence_before_sync();
+          __syncwarp();
+          if (lane_id == 0) tc::mbar_arrive(&bar_d_empty[eg]);
+        }
+        // 8 slots branch free (their phase chains interleave), all results
+        // computed before the stores; outputs whose window crosses the NCO
+        // rollover are written unrotated and fixed from that value below
+        uint32_t slow = 0, keep = 0;
+        float2 res[8];
+        uint64_t dst_a[8];
+        const uint32_t mbase = meta_s + (uint32_t)(cc * 8) * (uint32_t)sizeof(SlotMeta);
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
-          const int n = cc * 8 + e;
-          const bool valid = row_ok && n < n_hi;
-          const OutMeta& cm = meta[valid ? n : n_lo];
+          const int si = cc * 8 + e;
+          const uint32_t ma = mbase + (uint32_t)e * (uint32_t)sizeof(SlotMeta);
+          const uint4 h0 = lds_u4(ma);        // om_lo, om_hi, out
+          const uint4 h1 = lds_u4(ma + 16);   // R, T-1, U, r
+          const uint4 h2 = lds_u4(ma + 32);   // J, short_r, fastmod
+          const uint32_t P0 = __shfl_sync(0xffffffffu, si < 32 ? p0a : p0b, si & 31);
+          const uint32_t R = h1.x;
+          uint32_t pc = P0 + rowD;
+          if (h2.y) {  // short rollover (uniform over the warp): full reduction
+            const uint64_t fm = ((uint64_t)h2.w << 32) | h2.z;
+            pc = (uint32_t)__umul64hi(fm * (uint64_t)pc, (uint64_t)R);
+          } else {
+            pc = pc >= R ? pc - R : pc;
+          }
+          const bool okr = pc + h1.y < R;
+          // bits 32..63 of pc * omega64: the phase in 2^-32 turns
+          const uint32_t turns = __umulhi(pc, h0.x) + pc * h0.y;
+          const float ang = (float)(int32_t)turns * 1.4629180792671596e-09f;  // 2 pi / 2^32
+          float sn, cs;
+          __sincosf(ang, &sn, &cs);
           const float2 y0 = make_float2(__uint_as_float(v[2 * e]), __uint_as_float(v[2 * e + 1]));
-          float2 y = y0;
-          const bool okr = rotate_fast(cm, w0, T, y);
-          if (valid) cm.out[m] = okr ? y : y0;
+          const float2 y = cmul_nco(y0, make_float2(cs, sn));
+          const bool valid = j32 < (int32_t)h2.x;
+          const uint64_t m = (uint64_t)h1.w + (uint64_t)h1.z * (uint32_t)j32;
+          dst_a[e] = (((uint64_t)h0.w << 32) | h0.z) + m * sizeof(float2);
+          res[e] = okr ? y : y0;
+          keep |= valid ? (1u << e) : 0u;
           slow |= (valid && !okr) ? (1u << e) : 0u;
         }
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          if (keep & (1u << e)) *reinterpret_cast<float2*>(dst_a[e]) = res[e];
         while (slow) {
           const int e = __ffs(slow) - 1;
           slow &= slow - 1;
-          const int n = cc * 8 + e;
-          const OutMeta& cm = meta[n];
-          const ExactRot er = rotate_prep(cm, w0, T);
+          const SlotMeta& sm = meta[cc * 8 + e];
+          const int64_t w0 = (int64_t)sm.delta + j * D - sm.T + 1;
+          float2* dst = sm.nco.out + ((int64_t)sm.r + (int64_t)sm.U * j);
+          const ExactRot er = rotate_prep(sm.nco, w0, sm.T);
           float2 B = make_float2(0.f, 0.f);
           if (er.straddle) {
-            for (int k = er.k0; k < T; ++k) {
+            for (int k = er.k0; k < sm.T; ++k) {
               const float2 x = load_x(L, w0 + k);
-              const float2 gk = __ldg(W.taps32 + (size_t)k * W.n + n);
+              const float2 gk = __ldg(sm.taps32 + (size_t)k * sm.tstride + sm.tidx);
               B.x = fmaf(gk.x, x.x, B.x);
               B.x = fmaf(-gk.y, x.y, B.x);
               B.y = fmaf(gk.x, x.y, B.y);
               B.y = fmaf(gk.y, x.x, B.y);
             }
           }
-          cm.out[m] = rotate_apply(er, cm.out[m], B);
+          *dst = rotate_apply(er, *dst, B);
         }
       }
-      itr = item_next(L, G, itr);
-      ++it;
     }
-    if (failed && tid == 160) atomicExch(L.err, 1);
+    if (failed && lane_id == 0) atomicExch(L.err, 1);
   }
 
   // teardown: once every role has left its loop, every MMA this CTA issued
@@ -506,9 +595,15 @@ void PolyEngine::free_tc() {
   d_err_ = nullptr;
 }
 
-// Chunks of <= 64 channels per class (sorted by taps per phase), B operands in
-// the tcgen05 K-major no-swizzle layout for every phase, FP32 modulated taps
-// for the rollover correction.
+// Chunks of <= 32 channels per class (sorted by taps per phase).  For every
+// phase, B records in the K-major no-swizzle core layout: core (cg, t) of 8
+// columns x 1 tap at byte (cg T + t) 128, column c of the core at c 16,
+// element e at e 2.  Column 2i is Re, 2i+1 Im of channel i; with the input
+// record [xr_h, xi_h, xr_l, xi_l, xr_h, xi_h, xr_l, xi_l] the elements are
+//     Re: [gr_h, -gi_h, gr_h, -gi_h, gr_l, -gi_l, gr_l, -gi_l]
+//     Im: [gi_h,  gr_h, gi_h,  gr_h, gi_l,  gr_l, gi_l,  gr_l]
+// so each column sums (xh + xl)(gh + gl) over re/im.  Also the FP32
+// modulated taps for the rollover correction.
 int PolyEngine::build_tc(int fmt) {
   free_tc();
   tc_fmt_ = fmt;
@@ -516,17 +611,16 @@ int PolyEngine::build_tc(int fmt) {
     const EngineClass& k = classes_[ki];
     std::vector<int> cs = k.chans;
     std::stable_sort(cs.begin(), cs.end(), [&](int a, int b) { return chans_[a].T > chans_[b].T; });
-    for (size_t i0 = 0; i0 < cs.size(); i0 += 64) {
+    for (size_t i0 = 0; i0 < cs.size(); i0 += kTcChunk) {
       TcChunk ch;
       ch.cls = (int)ki;
-      ch.chans.assign(cs.begin() + i0, cs.begin() + std::min(cs.size(), i0 + 64));
+      ch.chans.assign(cs.begin() + i0, cs.begin() + std::min(cs.size(), i0 + (size_t)kTcChunk));
       const int n = (int)ch.chans.size();
       const int tmax = (int)chans_[ch.chans[0]].T;
-      ch.T = (tmax + 7) & ~7;
-      ch.supported = ch.T <= 64;
-      ch.N_pad = ((2 * n + 15) / 16) * 16;
-      const int Kp = 2 * ch.T;
-      ch.bbytes = ch.N_pad * Kp * 2;
+      ch.T = (tmax + 1) & ~1;
+      ch.supported = ch.T <= kTcMaxTaps;
+      ch.ng = (2 * n + 7) / 8;
+      ch.bbytes = (size_t)ch.ng * ch.T * 128;
       ch.d_b = nullptr;
       ch.d_taps32 = nullptr;
       ch.d_ch = nullptr;
@@ -535,7 +629,7 @@ int PolyEngine::build_tc(int fmt) {
         continue;
       }
       const uint32_t U = k.up;
-      std::vector<uint8_t> bh((size_t)U * 2 * ch.bbytes, 0);
+      std::vector<uint8_t> bh((size_t)U * ch.bbytes, 0);
       std::vector<float2> t32((size_t)U * ch.T * n, make_float2(0.f, 0.f));
       for (int ci = 0; ci < n; ++ci) {
         const EngineChannel& e = chans_[ch.chans[ci]];
@@ -546,8 +640,7 @@ int PolyEngine::build_tc(int fmt) {
           if (fm < 0) fm += fs_;
         }
         for (uint32_t ph = 0; ph < U; ++ph) {
-          uint8_t* bhi = bh.data() + (size_t)ph * 2 * ch.bbytes;
-          uint8_t* blo = bhi + ch.bbytes;
+          uint8_t* bp = bh.data() + (size_t)ph * ch.bbytes;
           for (int kk = pad; kk < ch.T; ++kk) {
             const float2 h = e.flipped[(size_t)ph * e.T + (kk - pad)];
             double gr = h.x, gi = h.y;
@@ -560,19 +653,16 @@ int PolyEngine::build_tc(int fmt) {
             }
             const float fr = (float)gr, fi = (float)gi;
             t32[((size_t)ph * ch.T + kk) * n + ci] = make_float2(fr, fi);
-            // columns: 2ci -> Re(y) = sum gr*xr - gi*xi ; 2ci+1 -> Im(y) = sum gi*xr + gr*xi
-            const float col[2][2] = {{fr, -fi}, {fi, fr}};
+            const uint16_t rh = to16(fr, fmt), ih = to16(fi, fmt);
+            const uint16_t rl = to16(fr - from16(rh, fmt), fmt), il = to16(fi - from16(ih, fmt), fmt);
+            const uint16_t sgn = 0x8000u;
+            const uint16_t re_col[8] = {rh, (uint16_t)(ih ^ sgn), rh, (uint16_t)(ih ^ sgn),
+                                        rl, (uint16_t)(il ^ sgn), rl, (uint16_t)(il ^ sgn)};
+            const uint16_t im_col[8] = {ih, rh, ih, rh, il, rl, il, rl};
             for (int part = 0; part < 2; ++part) {
-              const int nn = 2 * ci + part;
-              for (int ri = 0; ri < 2; ++ri) {
-                const int kp = 2 * kk + ri;
-                const size_t off = (size_t)(nn / 8) * (16 * Kp) + (size_t)(kp / 8) * 128 + (nn % 8) * 16 + (kp % 8) * 2;
-                const float v = col[part][ri];
-                const uint16_t hv = to16(v, fmt);
-                const uint16_t lv = to16(v - from16(hv, fmt), fmt);
-                std::memcpy(bhi + off, &hv, 2);
-                std::memcpy(blo + off, &lv, 2);
-              }
+              const int col = 2 * ci + part;
+              uint8_t* core = bp + ((size_t)(col / 8) * ch.T + kk) * 128 + (col % 8) * 16;
+              std::memcpy(core, part ? im_col : re_col, 16);
             }
           }
         }
@@ -638,108 +728,251 @@ int PolyEngine::prepare_tc_input(const float2* d_in, uint64_t n, cudaStream_t st
   return FDSP_OK;
 }
 
-int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream) {
-  static thread_local TcLaunch L;
-  std::memset(&L, 0, sizeof(L));
-  L.block = d_in;
-  L.hist = d_hist_[hist_cur_];
-  L.xhl = d_xhl_;
-  L.N = (int64_t)n;
-  L.H = H_;
-  L.nco = d_nco_;
-  L.err = d_err_;
-  for (size_t c = 0; c < chans_.size(); ++c) {
-    L.out[c] = out[c];
-    const uint32_t R = chans_[c].nco.rollover;
-    L.nco_base[c] = R ? (uint32_t)(abs0_ % R) : 0u;
+namespace {
+
+// One work set of the group for this apply, before merging.
+struct TcWsPlan {
+  const TcChunk* ch;
+  uint32_t phi;   // tap phase
+  int64_t delta;  // window end of row 0
+  int64_t J;
+  uint32_t U, r;
+};
+
+struct TcMsetPlan {
+  std::vector<int> ws;   // indices into the work-set list
+  int64_t E = 0;         // latest window end
+  int64_t S = 0;         // merged window start (row 0)
+  int Kw = 0;
+  int cols = 0;          // 8-column groups x 8
+};
+
+struct TcLaunchPlan {
+  std::vector<int> ms;   // merge-set indices
+  int64_t B0 = 0;
+  int V = 0, Qp = 0, wrap = 0, nbuf = 1;
+  size_t b_bytes = 0, meta_bytes = 0, tab_bytes = 0, in_bytes = 0;
+};
+
+// [B of each merge set | slot constants | A-offset tables | input buffers]
+size_t tc_smem_need(const TcLaunchPlan& p, int nbuf) {
+  return ((p.b_bytes + p.meta_bytes + p.tab_bytes + 127) & ~(size_t)127) + (size_t)nbuf * p.in_bytes;
+}
+
+// Staging geometry of a launch covering merge sets p.ms.
+void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t D) {
+  p.B0 = INT64_MAX;
+  p.b_bytes = p.meta_bytes = p.tab_bytes = 0;
+  for (int m : p.ms) {
+    p.B0 = std::min(p.B0, msets[m].S);
+    const int N = ((msets[m].cols + 15) / 16) * 16;
+    p.b_bytes += (size_t)N * msets[m].Kw * 16;
+    p.meta_bytes += (size_t)(N / 2) * sizeof(SlotMeta);
+    p.tab_bytes += (size_t)((msets[m].Kw / 2 + 3) & ~3) * 4;
   }
+  int64_t W = 0;
+  for (int m : p.ms) W = std::max<int64_t>(W, msets[m].S - p.B0 + msets[m].Kw);
+  p.wrap = W > (int64_t)D ? 1 : 0;
+  p.V = p.wrap ? (int)D + 1 : (int)W;
+  p.Qp = p.wrap ? 128 + (int)((W - 1) / D) : 128;
+  p.in_bytes = (((size_t)p.V * p.Qp * 16) + 127) & ~(size_t)127;
+}
+
+// Merge sets: consecutive (by window end) work sets while N <= cap columns
+// and the merged window stays within kTcMaxKw taps.
+std::vector<TcMsetPlan> tc_merge(const std::vector<TcWsPlan>& wl, const std::vector<int>& order, int cap) {
+  std::vector<TcMsetPlan> msets;
+  for (int wi : order) {
+    const TcWsPlan& w = wl[wi];
+    const int64_t s = w.delta - w.ch->T + 1;
+    const int cols = 8 * w.ch->ng;
+    bool joined = false;
+    if (!msets.empty()) {
+      TcMsetPlan& m = msets.back();
+      const int64_t E = std::max(m.E, w.delta);
+      const int64_t S = std::min(m.S, s);
+      const int Kw = (int)(((E - S + 1) + 1) & ~1LL);
+      if (m.cols + cols <= cap && Kw <= kTcMaxKw) {
+        m.ws.push_back(wi);
+        m.E = E;
+        m.S = E - Kw + 1;
+        m.Kw = Kw;
+        m.cols += cols;
+        joined = true;
+      }
+    }
+    if (!joined) {
+      TcMsetPlan m;
+      m.ws.push_back(wi);
+      m.E = w.delta;
+      m.Kw = w.ch->T;
+      m.S = m.E - m.Kw + 1;
+      m.cols = cols;
+      msets.push_back(m);
+    }
+  }
+  return msets;
+}
+
+// Launches: consecutive merge sets while shared memory allows; false when a
+// single merge set does not fit.
+bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, std::vector<TcLaunchPlan>& plans) {
+  plans.clear();
+  for (int mi = 0; mi < (int)msets.size(); ++mi) {
+    bool joined = false;
+    if (!plans.empty() && (int)plans.back().ms.size() < kMaxTcMsets) {
+      TcLaunchPlan p = plans.back();
+      p.ms.push_back(mi);
+      tc_geometry(msets, p, D);
+      if (tc_smem_need(p, 1) <= kTcSmemMax) {
+        plans.back() = p;
+        joined = true;
+      }
+    }
+    if (!joined) {
+      TcLaunchPlan p;
+      p.ms.push_back(mi);
+      tc_geometry(msets, p, D);
+      if (tc_smem_need(p, 1) > kTcSmemMax) return false;
+      plans.push_back(p);
+    }
+  }
+  for (auto& p : plans) {
+    p.nbuf = 1;
+    while (p.nbuf < kTcMaxBuf && tc_smem_need(p, p.nbuf + 1) <= kTcSmemMax) p.nbuf++;
+  }
+  return true;
+}
+
+}  // namespace
+
+int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream) {
   const EngineGroup& g = groups_[gi];
-  TcGroup& gd = L.groups[0];
-  gd.D = (int32_t)g.D;
-  gd.ws_begin = 0;
-  int nws = 0;
-  int64_t rows = 0;
-  int dmin = INT32_MAX, dmax = INT32_MIN, tmax = 8;
-  size_t off = 0;  // shared-memory layout: B of every work set, then constants, then input
+  const uint32_t D = g.D;
+  // ---- work sets of this apply (chunk x output phase r)
+  std::vector<TcWsPlan> wl;
   for (const auto& ch : tc_chunks_) {
     const EngineClass& k = classes_[ch.cls];
-    if (k.down != g.D) continue;
+    if (k.down != D) continue;
     const uint32_t U = k.up;
     for (uint32_t r = 0; r < U; ++r) {
       if (k.M <= r) continue;
-      const uint64_t J = (k.M - r + U - 1) / U;
-      const uint64_t t = (uint64_t)k.phase + (uint64_t)r * g.D;
-      const uint64_t delta = k.xoffset + t / U;
-      const uint32_t phi = (uint32_t)(t % U);
-      if (nws >= kMaxTcWorkSets) return FDSP_ERR_UNSUPPORTED;
-      TcWorkSet& W = L.ws[nws++];
-      W.bhi = ch.d_b + (size_t)phi * 2 * ch.bbytes;
-      W.blo = W.bhi + ch.bbytes;
-      W.taps32 = ch.d_taps32 + (size_t)phi * ch.T * ch.chans.size();
-      W.ch = ch.d_ch;
-      W.T = ch.T;
-      W.N_pad = ch.N_pad;
-      W.n = (int32_t)ch.chans.size();
-      W.delta = (int32_t)delta;
-      W.J = (int32_t)J;
-      W.U = (int32_t)U;
-      W.r = (int32_t)r;
-      W.bbytes = ch.bbytes;
-      W.ntiles = (int32_t)((J + 127) / 128);
-      W.boff = (int32_t)off;
-      off += (size_t)2 * ch.bbytes;
-      rows = std::max<int64_t>(rows, (int64_t)J);
-      dmin = std::min(dmin, (int)delta);
-      dmax = std::max(dmax, (int)delta);
-      tmax = std::max(tmax, ch.T);
+      const uint64_t t = (uint64_t)k.phase + (uint64_t)r * D;
+      TcWsPlan w;
+      w.ch = &ch;
+      w.phi = (uint32_t)(t % U);
+      w.delta = (int64_t)(k.xoffset + t / U);
+      w.J = (int64_t)((k.M - r + U - 1) / U);
+      w.U = U;
+      w.r = r;
+      wl.push_back(w);
     }
   }
-  gd.ws_end = nws;
-  L.ngroups = 1;
-  if (nws == 0) return FDSP_OK;
-  for (int wi = 0; wi < nws; ++wi) {
-    L.ws[wi].moff = (int32_t)off;
-    off += (size_t)L.ws[wi].n * sizeof(TcMeta);
+  if (wl.empty()) return FDSP_OK;
+  if ((int)wl.size() > kMaxTcWorkSets) return FDSP_ERR_UNSUPPORTED;
+  std::vector<int> order(wl.size());
+  for (size_t i = 0; i < wl.size(); ++i) order[i] = (int)i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return wl[a].delta < wl[b].delta; });
+  // ---- merge sets and launches; narrower merge sets when a wide one's B
+  // and input tile do not fit in shared memory together
+  std::vector<TcMsetPlan> msets;
+  std::vector<TcLaunchPlan> plans;
+  bool fits = false;
+  for (int cap = (int)kTcDCols; cap >= 16 && !fits; cap /= 2) {
+    msets = tc_merge(wl, order, cap);
+    fits = tc_pack(msets, D, plans);
   }
-  off = (off + 127) & ~(size_t)127;
-  gd.in_off = (int32_t)off;
-  gd.ntiles = (int32_t)((rows + 127) / 128);
-  gd.tmax = tmax;
-  gd.delta_min = dmin;
-  gd.delta_span = dmax - dmin;
-  // input staging: the whole tile de-interleaved by D when it is small (dense
-  // decimation, windows overlap), else each row's window in a double buffer
-  const int64_t len = 127LL * g.D + gd.delta_span + tmax;
-  int64_t P = (len + g.D - 1) / g.D;
-  if ((P & 1) == 0) P++;
-  gd.P = (int32_t)P;
-  gd.win_pitch = tmax + 1;  // odd pitch: two-way (minimal) bank use for 8-byte rows
-  gd.tile_elems = (int32_t)(((int64_t)g.D * P + 15) & ~15LL);  // one tile buffer (uint2), 128-byte multiple
-  const size_t deint_bytes = (size_t)2 * gd.tile_elems * sizeof(uint2);  // double buffered
-  const size_t win_bytes = (size_t)2 * 128 * gd.win_pitch * sizeof(float2);
-  const bool deint = deint_bytes <= win_bytes;
-  const size_t smem = std::max<size_t>(off + (deint ? deint_bytes : win_bytes), 120 * 1024);
-  if (smem > 225 * 1024) return FDSP_ERR_UNSUPPORTED;
-  // persistent: one CTA per SM (at least 120 KB of shared memory and all 512
-  // TMEM columns each, so two never share an SM), tiles strided over CTAs
+  if (!fits) return FDSP_ERR_UNSUPPORTED;
   if (num_sms_ == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev);
     if (num_sms_ <= 0) num_sms_ = 1;
   }
-  const int grid = std::max(1, std::min(num_sms_, (int)gd.ntiles));
-  void (*kern)(const TcLaunch, int);
-  if (tc_fmt_ == 0)
-    kern = deint ? poly_tc_kernel<0, true> : poly_tc_kernel<0, false>;
-  else
-    kern = deint ? poly_tc_kernel<1, true> : poly_tc_kernel<1, false>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return cuda_status(e);
-  kern<<<(unsigned)grid, kTcThreads, smem, stream>>>(L, 0);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_status(e);
-  launches_last_++;
+  // ---- fill and launch
+  static thread_local TcLaunch L;
+  for (const auto& p : plans) {
+    std::memset(&L, 0, sizeof(L));
+    L.block = d_in;
+    L.hist = d_hist_[hist_cur_];
+    L.xhl = d_xhl_;
+    L.nco = d_nco_;
+    L.err = d_err_;
+    L.N = (int64_t)n;
+    L.H = H_;
+    L.D = (int32_t)D;
+    for (size_t c = 0; c < chans_.size(); ++c) {
+      L.out[c] = out[c];
+      const uint32_t R = chans_[c].nco.rollover;
+      L.nco_base[c] = R ? (uint32_t)(abs0_ % R) : 0u;
+    }
+    size_t off = 0;
+    int nws = 0;
+    int64_t rows = 0;
+    L.nmsets = (int32_t)p.ms.size();
+    for (size_t q = 0; q < p.ms.size(); ++q) {
+      const TcMsetPlan& m = msets[p.ms[q]];
+      TcMset& M = L.ms[q];
+      M.Kw = m.Kw;
+      M.N = ((m.cols + 15) / 16) * 16;
+      M.a = (int32_t)(m.S - p.B0);
+      M.boff = (int32_t)off;
+      off += (size_t)M.N * M.Kw * 16;
+      M.ws_begin = nws;
+      int cg = 0;
+      for (int wi : m.ws) {
+        const TcWsPlan& w = wl[wi];
+        TcWorkSet& W = L.ws[nws++];
+        W.b = w.ch->d_b + (size_t)w.phi * w.ch->bbytes;
+        W.taps32 = w.ch->d_taps32 + (size_t)w.phi * w.ch->T * w.ch->chans.size();
+        W.ch = w.ch->d_ch;
+        W.T = w.ch->T;
+        W.n = (int32_t)w.ch->chans.size();
+        W.ng = w.ch->ng;
+        W.delta = (int32_t)w.delta;
+        W.J = (int32_t)w.J;
+        W.U = (int32_t)w.U;
+        W.r = (int32_t)w.r;
+        W.o = (int32_t)((w.delta - w.ch->T + 1) - m.S);
+        W.cg0 = cg;
+        cg += w.ch->ng;
+        rows = std::max(rows, w.J);
+      }
+      M.ws_end = nws;
+    }
+    for (size_t q = 0; q < p.ms.size(); ++q) {
+      L.ms[q].moff = (int32_t)off;
+      off += (size_t)(L.ms[q].N / 2) * sizeof(SlotMeta);
+    }
+    L.tab_off = (int32_t)off;
+    int toff = 0;
+    for (size_t q = 0; q < p.ms.size(); ++q) {
+      L.ms[q].toff = toff;
+      toff += (L.ms[q].Kw / 2 + 3) & ~3;
+    }
+    off += (size_t)toff * 4;
+    off = (off + 127) & ~(size_t)127;
+    L.in_off = (int32_t)off;
+    L.in_bytes = (int32_t)p.in_bytes;
+    L.nbuf = p.nbuf;
+    L.V = p.V;
+    L.Qp = p.Qp;
+    L.wrap = p.wrap;
+    L.B0 = (int32_t)p.B0;
+    L.ntiles = (int32_t)((rows + 127) / 128);
+    if (L.ntiles == 0) continue;
+    const size_t smem = off + (size_t)p.nbuf * p.in_bytes;
+    if (smem > kTcSmemMax) return FDSP_ERR_UNSUPPORTED;
+    const int grid = std::max(1, std::min(num_sms_, (int)L.ntiles));
+    void (*kern)(const TcLaunch) = tc_fmt_ == 0 ? poly_tc_kernel<0> : poly_tc_kernel<1>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e);
+    kern<<<(unsigned)grid, kTcThreads, smem, stream>>>(L);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+    launches_last_++;
+  }
+  tc_groups_last_++;
   return FDSP_OK;
 }
 

@@ -86,50 +86,61 @@ struct PolyLaunch {
 };
 
 // ---------------------------------------------------------------------------
-// Tensor-core launch (one decimation group per launch).
+// Tensor-core launch: a set of merge sets of one decimation group.
 // ---------------------------------------------------------------------------
 constexpr int kMaxTcWorkSets = 192;
+constexpr int kMaxTcMsets = 16;
 
+// One work set (chunk of channels of one (up, down) class x output phase r).
 struct TcWorkSet {
-  const uint8_t* bhi;    // B hi part, tcgen05 K-major no-swizzle layout (device)
-  const uint8_t* blo;    // B lo part
+  const uint8_t* b;      // B records of the work set's tap phase: [ng][T] cores of 128 B (device)
   const float2* taps32;  // [T][n] FP32 modulated taps (rollover correction)
   const int16_t* ch;     // channel ids of the chunk (device)
-  int32_t T;             // padded taps per phase (multiple of 8, <= 64)
-  int32_t N_pad;         // MMA N = 2 n rounded up to 16
+  int32_t T;             // taps per phase, padded to even
   int32_t n;             // channels in the chunk
+  int32_t ng;            // 8-column groups of its B (2 columns per channel)
   int32_t delta;         // window end of row 0 (block relative)
   int32_t J;             // rows with an output in this launch
-  int32_t U;
+  int32_t U;             // class up rate (output m = r + U j)
   int32_t r;
-  int32_t bbytes;        // bytes of one B part
-  int32_t ntiles;        // 128-row tiles of this work set
-  int32_t boff;          // shared-memory byte offset of this work set's B (hi, then lo)
-  int32_t moff;          // shared-memory byte offset of its channel constants
+  int32_t o;             // tap offset of its window inside the merge set's window
+  int32_t cg0;           // first 8-column group inside the merge set's B
   int32_t pad_;
 };
 
-struct TcGroup {
-  int32_t D, ws_begin, ws_end, ntiles;
-  int32_t in_off;        // shared-memory byte offset of the staged input
-  int32_t P;             // de-interleaved tile pitch (float2), tile-staging mode
-  int32_t tmax;          // longest padded window of the group
-  int32_t delta_min;     // smallest window-end offset of the group's work sets
-  int32_t delta_span;    // largest minus smallest
-  int32_t win_pitch;     // per-row window pitch (float2), window-staging mode
-  int32_t tile_elems;    // elements of one (double-buffered) de-interleaved tile
+// Work sets whose windows are merged into one wider matrix product: their
+// taps sit at their own offsets of a common window of Kw taps (zeros
+// elsewhere) and their channels side by side along N.
+struct TcMset {
+  int32_t Kw;            // taps of the merged window (even)
+  int32_t N;             // MMA N: columns, multiple of 16, <= 128
+  int32_t a;             // window start of row 0 inside the staged tile (records)
+  int32_t boff;          // shared-memory byte offset of its B
+  int32_t moff;          // shared-memory byte offset of its channel-slot constants
+  int32_t ws_begin, ws_end;
+  int32_t toff;          // first entry of its A-offset table (multiple of 4)
 };
 
 struct TcLaunch {
   const float2* block;
   const float2* hist;
   const uint2* xhl;                  // [history | block] as packed {hi, lo} 16-bit pairs
-  int64_t N;
-  int32_t H;
-  int32_t ngroups;
   const NcoConst* nco;
   int* err;                          // set to 1 when a bounded wait gave up
-  TcGroup groups[kMaxGroups];
+  int64_t N;
+  int32_t H;
+  int32_t D;
+  int32_t ntiles;                    // 128-row tiles
+  int32_t nmsets;
+  int32_t V;                         // staged phases per tile
+  int32_t Qp;                        // records per staged phase
+  int32_t wrap;                      // 1: a tap's phase is taken mod D (V = D + 1)
+  int32_t B0;                        // block-relative sample of record (0, 0) of tile 0
+  int32_t in_off;                    // shared-memory byte offset of the input buffers
+  int32_t in_bytes;                  // bytes of one input buffer
+  int32_t nbuf;                      // input buffers (1 to 4)
+  int32_t tab_off;                   // shared-memory byte offset of the A-offset tables
+  TcMset ms[kMaxTcMsets];
   TcWorkSet ws[kMaxTcWorkSets];
   float2* out[kMaxChannels];
   uint32_t nco_base[kMaxChannels];
@@ -140,12 +151,12 @@ static_assert(sizeof(TcLaunch) <= 32764, "tensor-core launch must fit the kernel
 struct TcChunk {
   int cls;
   std::vector<int> chans;
-  int T;          // padded taps per phase
-  bool supported; // T <= 64
-  int N_pad;
-  int bbytes;
-  uint8_t* d_b;   // [U][hi|lo][bbytes]
-  float2* d_taps32;
+  int T;            // taps per phase, padded to even
+  bool supported;   // T within the tensor-core kernel's limit
+  int ng;           // 8-column groups
+  size_t bbytes;    // bytes of one phase's B: ng * T * 128
+  uint8_t* d_b;     // [U][ng][T] cores of 128 B
+  float2* d_taps32; // [U][T][n]
   int16_t* d_ch;
 };
 
@@ -211,6 +222,9 @@ class PolyEngine {
   int nb() const { return nb_; }
   // Kernel launches enqueued by the most recent apply.
   int kernel_launches_last() const { return launches_last_; }
+  // Decimation groups computed by the tensor-core kernel in the most recent
+  // apply (the others took the FP32 kernel).
+  int tc_groups_last() const { return tc_groups_last_; }
 
   // Arithmetic of the filter-bank contraction: FDSP_PRECISION_FP32 (SIMT FP32)
   // or one of the split-precision tensor-core forms.
@@ -251,6 +265,7 @@ class PolyEngine {
   int hist_cur_ = 0;
   uint64_t abs0_ = 0;               // samples since reset at the next block
   int launches_last_ = 0;
+  int tc_groups_last_ = 0;
 };
 
 // NCO constants of a (fs, f) pair, following falcon_dsp_freq_shift.cc:194-235.
