@@ -68,8 +68,8 @@ constexpr size_t kTcSmemMax = 225 * 1024;
 constexpr int kTcMaxBuf = 4;          // input buffers
 
 // Constants of one channel slot (Re/Im column pair) of a merge set, staged
-// in shared memory.  The first 48 bytes are read for every output (three
-// 16-byte loads); the rest only once per item and on the exact path.
+// in shared memory: read once per item (row-0 counter) and on the exact
+// path; the per-output constants are in the kernel parameters (TcSlotHot).
 struct SlotMeta {
   uint32_t om_lo, om_hi;  // NCO turns per sample (2^-64 units; 0: no shift)
   float2* out;            // output base of the channel
@@ -87,15 +87,6 @@ struct SlotMeta {
   int32_t pad_[2];
 };
 static_assert(sizeof(SlotMeta) == 128, "slot constants layout");
-
-// Shared-memory load of read-only slot constants: plain (non-volatile) asm
-// without a memory clobber, so the compiler may hoist it above the output
-// stores of earlier slots (they cannot alias).
-__device__ __forceinline__ uint4 lds_u4(uint32_t a) {
-  uint4 v;
-  asm("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
-  return v;
-}
 
 __device__ __forceinline__ float2 load_x(const TcLaunch& L, int64_t v) {
   if (v < 0) {
@@ -447,7 +438,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       tc::fence_after_sync();
       const TcMset& M = L.ms[mi];
       const SlotMeta* meta = reinterpret_cast<const SlotMeta*>(smem + M.moff);
-      const uint32_t meta_s = tc::smem_u32(smem + M.moff);
       const int nslots = M.N >> 1;
       const int64_t j0 = (int64_t)tile * 128;
       const int64_t j = j0 + row;
@@ -490,34 +480,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         uint32_t slow = 0, keep = 0;
         float2 res[8];
         uint64_t dst_a[8];
-        const uint32_t mbase = meta_s + (uint32_t)(cc * 8) * (uint32_t)sizeof(SlotMeta);
+        const TcSlotHot* hot = L.slot + M.slot0 + cc * 8;
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
           const int si = cc * 8 + e;
-          const uint32_t ma = mbase + (uint32_t)e * (uint32_t)sizeof(SlotMeta);
-          const uint4 h0 = lds_u4(ma);        // om_lo, om_hi, out
-          const uint4 h1 = lds_u4(ma + 16);   // R, T-1, U, r
-          const uint4 h2 = lds_u4(ma + 32);   // J, short_r, fastmod
+          const TcSlotHot sh = hot[e];
           const uint32_t P0 = __shfl_sync(0xffffffffu, si < 32 ? p0a : p0b, si & 31);
-          const uint32_t R = h1.x;
+          const uint32_t R = sh.R;
           uint32_t pc = P0 + rowD;
-          if (h2.y) {  // short rollover (uniform over the warp): full reduction
-            const uint64_t fm = ((uint64_t)h2.w << 32) | h2.z;
+          if (sh.ur >> 31) {  // short rollover (uniform over the warp): full reduction
+            const uint64_t fm = meta[si].fastmod;
             pc = (uint32_t)__umul64hi(fm * (uint64_t)pc, (uint64_t)R);
           } else {
             pc = pc >= R ? pc - R : pc;
           }
-          const bool okr = pc + h1.y < R;
+          const bool okr = pc + sh.Tm1 < R;
           // bits 32..63 of pc * omega64: the phase in 2^-32 turns
-          const uint32_t turns = __umulhi(pc, h0.x) + pc * h0.y;
+          const uint32_t turns = __umulhi(pc, sh.om_lo) + pc * sh.om_hi;
           const float ang = (float)(int32_t)turns * 1.4629180792671596e-09f;  // 2 pi / 2^32
           float sn, cs;
           __sincosf(ang, &sn, &cs);
           const float2 y0 = make_float2(__uint_as_float(v[2 * e]), __uint_as_float(v[2 * e + 1]));
           const float2 y = cmul_nco(y0, make_float2(cs, sn));
-          const bool valid = j32 < (int32_t)h2.x;
-          const uint64_t m = (uint64_t)h1.w + (uint64_t)h1.z * (uint32_t)j32;
-          dst_a[e] = (((uint64_t)h0.w << 32) | h0.z) + m * sizeof(float2);
+          const bool valid = j32 < sh.J;
+          const uint64_t m = (uint64_t)((sh.ur >> 16) & 0x7fffu) + (uint64_t)(sh.ur & 0xffffu) * (uint32_t)j32;
+          dst_a[e] = (((uint64_t)sh.out_hi << 32) | sh.out_lo) + m * sizeof(float2);
           res[e] = okr ? y : y0;
           keep |= valid ? (1u << e) : 0u;
           slow |= (valid && !okr) ? (1u << e) : 0u;
@@ -618,7 +605,7 @@ int PolyEngine::build_tc(int fmt) {
       const int n = (int)ch.chans.size();
       const int tmax = (int)chans_[ch.chans[0]].T;
       ch.T = (tmax + 1) & ~1;
-      ch.supported = ch.T <= kTcMaxTaps;
+      ch.supported = ch.T <= kTcMaxTaps && k.up < 32768u;  // U and r packed in 16 / 15 bits
       ch.ng = (2 * n + 7) / 8;
       ch.bbytes = (size_t)ch.ng * ch.T * 128;
       ch.d_b = nullptr;
@@ -749,6 +736,7 @@ struct TcMsetPlan {
 
 struct TcLaunchPlan {
   std::vector<int> ms;   // merge-set indices
+  int nws = 0, nslots = 0;
   int64_t B0 = 0;
   int V = 0, Qp = 0, wrap = 0, nbuf = 1;
   size_t b_bytes = 0, meta_bytes = 0, tab_bytes = 0, in_bytes = 0;
@@ -763,9 +751,12 @@ size_t tc_smem_need(const TcLaunchPlan& p, int nbuf) {
 void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t D) {
   p.B0 = INT64_MAX;
   p.b_bytes = p.meta_bytes = p.tab_bytes = 0;
+  p.nws = p.nslots = 0;
   for (int m : p.ms) {
     p.B0 = std::min(p.B0, msets[m].S);
     const int N = ((msets[m].cols + 15) / 16) * 16;
+    p.nws += (int)msets[m].ws.size();
+    p.nslots += N / 2;
     p.b_bytes += (size_t)N * msets[m].Kw * 16;
     p.meta_bytes += (size_t)(N / 2) * sizeof(SlotMeta);
     p.tab_bytes += (size_t)((msets[m].Kw / 2 + 3) & ~3) * 4;
@@ -824,7 +815,7 @@ bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, std::vector<TcLau
       TcLaunchPlan p = plans.back();
       p.ms.push_back(mi);
       tc_geometry(msets, p, D);
-      if (tc_smem_need(p, 1) <= kTcSmemMax) {
+      if (tc_smem_need(p, 1) <= kTcSmemMax && p.nws <= kMaxTcWorkSets && p.nslots <= kMaxTcSlots) {
         plans.back() = p;
         joined = true;
       }
@@ -833,7 +824,7 @@ bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, std::vector<TcLau
       TcLaunchPlan p;
       p.ms.push_back(mi);
       tc_geometry(msets, p, D);
-      if (tc_smem_need(p, 1) > kTcSmemMax) return false;
+      if (tc_smem_need(p, 1) > kTcSmemMax || p.nws > kMaxTcWorkSets || p.nslots > kMaxTcSlots) return false;
       plans.push_back(p);
     }
   }
@@ -869,7 +860,6 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
     }
   }
   if (wl.empty()) return FDSP_OK;
-  if ((int)wl.size() > kMaxTcWorkSets) return FDSP_ERR_UNSUPPORTED;
   std::vector<int> order(wl.size());
   for (size_t i = 0; i < wl.size(); ++i) order[i] = (int)i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return wl[a].delta < wl[b].delta; });
@@ -939,6 +929,37 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
         rows = std::max(rows, w.J);
       }
       M.ws_end = nws;
+    }
+    // per-output slot constants (the same rules as the kernel's slot table)
+    int nslot = 0;
+    for (size_t q = 0; q < p.ms.size(); ++q) {
+      TcMset& M = L.ms[q];
+      M.slot0 = nslot;
+      for (int sI = 0; sI < M.N / 2; ++sI) {
+        TcSlotHot& h = L.slot[nslot++];
+        h.R = 0x7fffffffu;
+        for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
+          const TcWorkSet& W = L.ws[wi];
+          const int i = sI - 4 * W.cg0;
+          if (i < 0 || i >= 4 * W.ng) continue;
+          if (i < W.n) {
+            const TcWsPlan& w = wl[msets[p.ms[q]].ws[wi - M.ws_begin]];
+            const int c = w.ch->chans[i];
+            const NcoConst& nc = chans_[c].nco;
+            const bool general = nc.enabled && nc.rollover >= 0x80000000u;
+            const bool shortr = nc.enabled && !general && (uint64_t)nc.rollover <= 127ull * D + (uint64_t)W.T;
+            h.om_lo = nc.enabled && !general ? (uint32_t)nc.omega64 : 0u;
+            h.om_hi = nc.enabled && !general ? (uint32_t)(nc.omega64 >> 32) : 0u;
+            h.out_lo = (uint32_t)(uintptr_t)out[c];
+            h.out_hi = (uint32_t)((uintptr_t)out[c] >> 32);
+            h.R = nc.enabled && !general ? nc.rollover : 0x7fffffffu;
+            h.Tm1 = general ? 0x7fffffffu : (uint32_t)(W.T - 1);
+            h.ur = (uint32_t)W.U | ((uint32_t)W.r << 16) | (shortr ? 0x80000000u : 0u);
+            h.J = W.J;
+          }
+          break;
+        }
+      }
     }
     for (size_t q = 0; q < p.ms.size(); ++q) {
       L.ms[q].moff = (int32_t)off;

@@ -88,8 +88,9 @@ struct PolyLaunch {
 // ---------------------------------------------------------------------------
 // Tensor-core launch: a set of merge sets of one decimation group.
 // ---------------------------------------------------------------------------
-constexpr int kMaxTcWorkSets = 192;
+constexpr int kMaxTcWorkSets = 128;
 constexpr int kMaxTcMsets = 16;
+constexpr int kMaxTcSlots = 256;     // channel slots (Re/Im column pairs) per launch
 
 // One work set (chunk of channels of one (up, down) class x output phase r).
 struct TcWorkSet {
@@ -119,6 +120,20 @@ struct TcMset {
   int32_t moff;          // shared-memory byte offset of its channel-slot constants
   int32_t ws_begin, ws_end;
   int32_t toff;          // first entry of its A-offset table (multiple of 4)
+  int32_t slot0;         // first entry of its channel slots in TcLaunch::slot
+  int32_t pad_[3];
+};
+
+// Per-output constants of one channel slot, read by every output of the
+// slot (kernel parameters: served by the constant cache, so they take no
+// shared-memory bandwidth from the matrix operands).
+struct TcSlotHot {
+  uint32_t om_lo, om_hi;  // NCO turns per sample (2^-64 units; 0: no shift)
+  uint32_t out_lo, out_hi;// output base of the channel
+  uint32_t R;             // counter rollover (0x7fffffff: no shift, or exact path)
+  uint32_t Tm1;           // taps - 1 (0x7fffffff: every output on the exact path)
+  uint32_t ur;            // U | r << 16 | short rollover << 31 (output m = r + U j)
+  int32_t J;              // rows with an output (0: padding slot)
 };
 
 struct TcLaunch {
@@ -141,6 +156,7 @@ struct TcLaunch {
   int32_t nbuf;                      // input buffers (1 to 4)
   int32_t tab_off;                   // shared-memory byte offset of the A-offset tables
   TcMset ms[kMaxTcMsets];
+  TcSlotHot slot[kMaxTcSlots];
   TcWorkSet ws[kMaxTcWorkSets];
   float2* out[kMaxChannels];
   uint32_t nco_base[kMaxChannels];
