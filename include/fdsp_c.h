@@ -133,6 +133,19 @@ int fdsp_channelizer_kernel_launches(const fdsp_channelizer *h, uint32_t *n);
  * the tensor-core kernel's limits, or precision FP32).  No counterpart in the
  * reference, which has one arithmetic path. */
 int fdsp_channelizer_tc_groups(const fdsp_channelizer *h, uint32_t *n);
+/* Autotuner (no counterpart in the reference): times every decimation group
+ * (channels sharing a down rate) on an n_in-sample block on `stream` and keeps,
+ * per group, the fastest FP32 tile height and, under a tensor-core precision,
+ * the faster of the tensor-core and FP32 forms.  It allocates scratch for the
+ * trial, synchronises the stream and resets the streaming state; call it after
+ * fdsp_channelizer_set_precision and before the first apply. */
+int fdsp_channelizer_autotune(fdsp_channelizer *h, uint64_t n_in, fdsp_stream_t stream);
+/* Decimation groups of the channelizer and, per group, its down rate, FP32
+ * tile height (output rows per CTA) and whether applies ask for the
+ * tensor-core form for it. */
+int fdsp_channelizer_num_groups(const fdsp_channelizer *h, uint32_t *n);
+int fdsp_channelizer_group_info(const fdsp_channelizer *h, uint32_t group, uint32_t *down_rate, uint32_t *tile_rows,
+                                int *tensor_core);
 /* apply(in, out) on host buffers (copies in, computes, copies out, syncs). */
 int fdsp_channelizer_apply_host(fdsp_channelizer *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,
                                 const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);

@@ -160,6 +160,24 @@ class MultiRateChannelizerCuda(_Handle):
         _capi.call("fdsp_channelizer_kernel_launches", self._h, C.byref(v))
         return v.value
 
+    def autotune(self, n_in: int, stream: int | None = None) -> list[dict]:
+        """Time each decimation group on an n_in-sample block and keep the
+        fastest FP32 tile height and (tensor-core precisions) the faster
+        form per group; resets the streaming state.  Returns group_info()."""
+        s = _stream_handle() if stream is None else stream
+        _capi.call("fdsp_channelizer_autotune", self._h, int(n_in), C.c_void_p(s))
+        return self.group_info()
+
+    def group_info(self) -> list[dict]:
+        n = C.c_uint32()
+        _capi.call("fdsp_channelizer_num_groups", self._h, C.byref(n))
+        out = []
+        for g in range(n.value):
+            d, q, tcf = C.c_uint32(), C.c_uint32(), C.c_int()
+            _capi.call("fdsp_channelizer_group_info", self._h, g, C.byref(d), C.byref(q), C.byref(tcf))
+            out.append({"down_rate": d.value, "tile_rows": q.value, "tensor_core": bool(tcf.value)})
+        return out
+
     def tc_groups(self) -> int:
         """Decimation groups the last apply computed on the tensor-core kernel."""
         v = C.c_uint32()

@@ -71,6 +71,9 @@ SIGNATURES = {
     "fdsp_channelizer_apply_host": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
     "fdsp_channelizer_kernel_launches": [_vp, _pu32],
     "fdsp_channelizer_tc_groups": [_vp, _pu32],
+    "fdsp_channelizer_autotune": [_vp, _u64, _vp],
+    "fdsp_channelizer_num_groups": [_vp, _pu32],
+    "fdsp_channelizer_group_info": [_vp, _u32, _pu32, _pu32, C.POINTER(C.c_int)],
     "fdsp_channelizer_set_precision": [_vp, C.c_int],
     "fdsp_resampler_create": [_u32, _u32, _vp, _u32, _pp],
     "fdsp_resampler_destroy": [_vp],

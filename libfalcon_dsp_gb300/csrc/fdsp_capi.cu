@@ -247,6 +247,28 @@ int fdsp_channelizer_tc_groups(const fdsp_channelizer* h, uint32_t* n) {
   return FDSP_OK;
 }
 
+int fdsp_channelizer_autotune(fdsp_channelizer* h, uint64_t n_in, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return h->eng.autotune(n_in, (cudaStream_t)stream);
+}
+
+int fdsp_channelizer_num_groups(const fdsp_channelizer* h, uint32_t* n) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!n) return FDSP_ERR_INVALID_ARG;
+  *n = (uint32_t)h->eng.num_groups();
+  return FDSP_OK;
+}
+
+int fdsp_channelizer_group_info(const fdsp_channelizer* h, uint32_t group, uint32_t* down_rate, uint32_t* tile_rows,
+                                int* tensor_core) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!down_rate || !tile_rows || !tensor_core || group >= (uint32_t)h->eng.num_groups()) return FDSP_ERR_INVALID_ARG;
+  int qt = 0;
+  h->eng.group_info((int)group, down_rate, &qt, tensor_core);
+  *tile_rows = (uint32_t)qt;
+  return FDSP_OK;
+}
+
 int fdsp_channelizer_apply_host(fdsp_channelizer* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* const* h_out,
                                 const uint64_t* out_cap, uint64_t* n_out, fdsp_stream_t stream) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;

@@ -416,6 +416,7 @@ int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool
     for (int b : g.batches) tmax = std::max(tmax, batches_[b].T);
     g.Qt = choose_qt(g.D, tmax);
     if (g.Qt < 0) return FDSP_ERR_UNSUPPORTED;
+    g.Qt_default = g.Qt;
   }
 
   // modulated, padded taps of every batch: [up][T][NB]
@@ -513,6 +514,86 @@ int PolyEngine::set_precision(int mode) {
   if (st != FDSP_OK) return st;
   precision_ = mode;
   return FDSP_OK;
+}
+
+bool PolyEngine::use_tc_for(int eg) const {
+  if (precision_ == FDSP_PRECISION_FP32 || force_ == 0 || !group_tc_ok(eg)) return false;
+  return force_ == 1 || groups_[eg].use_tc != 0;
+}
+
+int PolyEngine::autotune(uint64_t n, cudaStream_t stream) {
+  if (n == 0 || n >= (1ull << 31)) return FDSP_ERR_INVALID_ARG;
+  const size_t ng = groups_.size();
+  float2* d_in = nullptr;
+  std::vector<float2*> outs(chans_.size(), nullptr);
+  int st = cuda_status(cudaMalloc(&d_in, n * sizeof(float2)));
+  if (st == FDSP_OK) st = cuda_status(cudaMemsetAsync(d_in, 0, n * sizeof(float2), stream));
+  for (size_t c = 0; c < chans_.size() && st == FDSP_OK; ++c) {
+    const uint64_t cap = (n * chans_[c].up + chans_[c].down - 1) / chans_[c].down + 2;
+    st = cuda_status(cudaMalloc(&outs[c], cap * sizeof(float2)));
+  }
+  prof_ev_.assign(2 * ng, nullptr);
+  prof_hit_.assign(ng, 0);
+  prof_tc_.assign(ng, 0);
+  for (size_t i = 0; i < prof_ev_.size() && st == FDSP_OK; ++i) st = cuda_status(cudaEventCreate(&prof_ev_[i]));
+  std::vector<uint64_t> counts(chans_.size());
+  // minimum over 3 timed applies (after one untimed) of each group's time
+  auto run = [&](int force, std::vector<float>& t) -> int {
+    t.assign(ng, 3.4e38f);
+    reset();
+    force_ = force;
+    for (int rep = 0; rep < 4; ++rep) {
+      std::fill(prof_hit_.begin(), prof_hit_.end(), 0);
+      int s2 = apply(d_in, n, outs.data(), nullptr, counts.data(), stream);
+      if (s2 == FDSP_OK) s2 = cuda_status(cudaStreamSynchronize(stream));
+      if (s2 != FDSP_OK) return s2;
+      if (rep == 0) continue;
+      for (size_t g = 0; g < ng; ++g) {
+        if (!prof_hit_[g]) continue;
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, prof_ev_[2 * g], prof_ev_[2 * g + 1]) == cudaSuccess) t[g] = std::min(t[g], ms);
+      }
+    }
+    return FDSP_OK;
+  };
+  std::vector<float> best(ng, 3.4e38f), t;
+  std::vector<int> best_qt(ng);
+  for (size_t g = 0; g < ng; ++g) best_qt[g] = groups_[g].Qt_default;
+  // FP32 tile height: the default, half and double where shared memory allows
+  const int factor_num[3] = {1, 1, 2}, factor_den[3] = {1, 2, 1};
+  for (int ci = 0; ci < 3 && st == FDSP_OK; ++ci) {
+    std::vector<char> valid(ng, 0);
+    for (size_t g = 0; g < ng; ++g) {
+      EngineGroup& eg = groups_[g];
+      const int q = (eg.Qt_default * factor_num[ci] / factor_den[ci]) & ~31;
+      const int64_t len = (int64_t)q * eg.D + 3LL * eg.D + 64;
+      valid[g] = q >= 32 && (int64_t)eg.D * (len / eg.D + 2) * 8 <= 200 * 1024;
+      eg.Qt = valid[g] ? q : eg.Qt_default;
+    }
+    st = run(0, t);
+    for (size_t g = 0; g < ng && st == FDSP_OK; ++g)
+      if (valid[g] && t[g] < best[g]) {
+        best[g] = t[g];
+        best_qt[g] = groups_[g].Qt;
+      }
+  }
+  for (size_t g = 0; g < ng; ++g) groups_[g].Qt = best_qt[g];
+  if (st == FDSP_OK && precision_ != FDSP_PRECISION_FP32) {
+    st = run(1, t);
+    // a group keeps the tensor-core form only where that kernel really ran
+    // (configurations beyond its limits fall back to FP32) and was faster
+    for (size_t g = 0; g < ng && st == FDSP_OK; ++g) groups_[g].use_tc = (prof_tc_[g] && t[g] < best[g]) ? 1 : 0;
+  }
+  force_ = -1;
+  for (auto ev : prof_ev_)
+    if (ev) cudaEventDestroy(ev);
+  prof_ev_.clear();
+  cudaStreamSynchronize(stream);
+  if (d_in) cudaFree(d_in);
+  for (auto p : outs)
+    if (p) cudaFree(p);
+  reset();
+  return st;
 }
 
 void PolyEngine::reset() {
@@ -616,7 +697,7 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
   // tensor-core groups read the input pre-split into {hi, lo} pairs
   if (precision_ != FDSP_PRECISION_FP32) {
     bool any_tc = false;
-    for (int gi = 0; gi < ng; ++gi) any_tc = any_tc || group_tc_ok(group_of_d_[L.groups[gi].D]);
+    for (int gi = 0; gi < ng; ++gi) any_tc = any_tc || use_tc_for(group_of_d_[L.groups[gi].D]);
     if (any_tc) {
       const int st = prepare_tc_input(d_in, n, stream);
       if (st != FDSP_OK) return st;
@@ -627,15 +708,24 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
   for (int gi = 0; gi < ng; ++gi) {
     const GroupDesc& gd = L.groups[gi];
     if (gd.ntiles <= 0) continue;
-    if (precision_ != FDSP_PRECISION_FP32) {
-      const int eg = group_of_d_[gd.D];
-      if (group_tc_ok(eg)) {
-        // groups whose operands do not fit the tensor-core kernel's shared
-        // memory keep the FP32 form (nothing was launched in that case)
-        const int st = launch_tc_group(eg, d_in, n, out, stream);
-        if (st == FDSP_OK) continue;
-        if (st != FDSP_ERR_UNSUPPORTED) return st;
+    const int eg = group_of_d_[gd.D];
+    if (!prof_ev_.empty()) {
+      cudaEventRecord(prof_ev_[2 * eg], stream);
+      prof_hit_[eg] = 1;
+    }
+    if (use_tc_for(eg)) {
+      // groups whose operands do not fit the tensor-core kernel's shared
+      // memory keep the FP32 form (nothing was launched in that case)
+      const int before = tc_groups_last_;
+      const int st = launch_tc_group(eg, d_in, n, out, stream);
+      if (st == FDSP_OK) {
+        if (!prof_ev_.empty()) {
+          cudaEventRecord(prof_ev_[2 * eg + 1], stream);
+          prof_tc_[eg] = tc_groups_last_ > before ? 1 : 0;
+        }
+        continue;
       }
+      if (st != FDSP_ERR_UNSUPPORTED) return st;
     }
     const size_t smem = (size_t)gd.smem_bytes;
     auto kern = gd.taps_smem ? poly_fp32_kernel<NB, true> : poly_fp32_kernel<NB, false>;
@@ -645,6 +735,10 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
+    if (!prof_ev_.empty()) {
+      cudaEventRecord(prof_ev_[2 * eg + 1], stream);
+      prof_tc_[eg] = 0;
+    }
   }
   if (H_ > 0) {
     hist_update_kernel<<<(H_ + 255) / 256, 256, 0, stream>>>(d_hist_[hist_cur_], d_in, (int64_t)n, H_,

@@ -211,6 +211,8 @@ struct EngineBatch {
 struct EngineGroup {
   uint32_t D;
   int Qt;
+  int Qt_default = 0;  // tile rows chosen from the shapes alone
+  int use_tc = 1;      // tensor-core form when the precision asks for it (autotuned)
   std::vector<int> batches;
 };
 
@@ -248,6 +250,16 @@ class PolyEngine {
   int precision() const { return precision_; }
   // 1 when a tensor-core kernel hit its bounded wait since the last reset.
   int tc_error() const;
+  // Time every decimation group on an n-sample block: the FP32 tile height
+  // among {1/2, 1, 2} x the default, then tensor cores vs FP32 under a
+  // tensor-core precision; keep the fastest per group.  Resets the stream.
+  int autotune(uint64_t n, cudaStream_t stream);
+  int num_groups() const { return (int)groups_.size(); }
+  void group_info(int g, uint32_t* D, int* Qt, int* use_tc) const {
+    *D = groups_[g].D;
+    *Qt = groups_[g].Qt;
+    *use_tc = use_tc_for(g) ? 1 : 0;
+  }
 
  private:
   template <int NB>
@@ -282,6 +294,11 @@ class PolyEngine {
   uint64_t abs0_ = 0;               // samples since reset at the next block
   int launches_last_ = 0;
   int tc_groups_last_ = 0;
+  int force_ = -1;                     // autotuning: -1 chosen forms, 0 all FP32, 1 all tensor cores
+  bool use_tc_for(int eg) const;
+  std::vector<cudaEvent_t> prof_ev_;   // autotuning: [2 g] / [2 g + 1] around group g
+  std::vector<int> prof_hit_;          // group g launched in the timed apply
+  std::vector<int> prof_tc_;           // group g ran on the tensor-core kernel
 };
 
 // NCO constants of a (fs, f) pair, following falcon_dsp_freq_shift.cc:194-235.

@@ -72,3 +72,24 @@ def test_tc_rollover_straddles_and_matches_fp32_path():
             if yc.size > 8:
                 assert snr_db(yb, yc) >= SNR_MIN_DB, snr_db(yb, yc)
                 assert snr_db(ya, yc) >= 100.0
+
+
+def test_autotune_keeps_results_and_streaming():
+    """The autotuner only picks tile heights and forms: outputs after it stay
+    within the tensor-core bound of the FP64 oracle, from a reset state, and
+    the groups it gives the tensor-core form run on the tensor-core kernel."""
+    torch = pytest.importorskip("torch")
+    fs = 61440000
+    chans = channelizer_256_plan(float(fs), [1.0e6, -3.0e6, 7.5e6, -12.0e6], 24, 5)
+    x, _ = tone_signal(1 << 16, float(fs), 64, seed=3)
+    g = F.MultiRateChannelizerCuda(fs, chans)
+    g.set_precision("fp16x3")
+    info = g.autotune(1 << 16)
+    assert len(info) == len({c["down_rate"] for c in chans})
+    assert all(i["tile_rows"] % 32 == 0 and i["tile_rows"] >= 32 for i in info)
+    ys = [y.cpu().numpy() for y in g.apply(torch.from_numpy(x).cuda())]
+    ref = O.Channelizer(fs, chans, precision="f64").apply(x)
+    for y, r in zip(ys, ref):
+        assert y.size == r.size
+        assert snr_db(y, r) >= SNR_MIN_DB
+    assert g.tc_groups() == sum(i["tensor_core"] for i in info)
