@@ -164,6 +164,20 @@ def cpu_channelizer_rate(fs, chans, x, threads, use_reference: bool) -> tuple[fl
     return tot / dt / 1e6, kind, threads
 
 
+def replica_aggregate(t, units, world: int, dev):
+    """Whole-job numbers of N independent replicas (no data exchange on the
+    path): the slowest rank's time and the units all ranks processed."""
+    if world <= 1:
+        return float(t), float(units)
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([float(t)], device=dev, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    uu = torch.tensor([float(units)], device=dev, dtype=torch.float64)
+    dist.all_reduce(uu)
+    return float(tt.item()), float(uu.item())
+
+
 # --------------------------------------------------------------------------- reference arm
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
@@ -285,15 +299,7 @@ def run_ours(args) -> None:
         fms = f0.elapsed_time(f1)
         plain = {"value": round(fo / (fms / 1e3) / 1e6, 1), "unit": "Msamples/s", "ms_per_step": round(fms / args.steps, 4)}
         ch.set_precision(args.precision)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        o = torch.tensor([float(outputs)], device=dev, dtype=torch.float64)
-        dist.all_reduce(o)
-        outputs_all = float(o.item())
-    else:
-        outputs_all = float(outputs)
+    ms, outputs_all = replica_aggregate(ms, outputs, world, dev)
     ms_per_step = ms / args.steps
     value = outputs_all / (ms / 1e3) / 1e6
 
@@ -334,13 +340,7 @@ def run_ours(args) -> None:
         for _ in range(args.e2e_steps):
             eo += step_host()
         dt = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([dt], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
-            o = torch.tensor([float(eo)], device=dev, dtype=torch.float64)
-            dist.all_reduce(o)
-            eo = float(o.item())
+        dt, eo = replica_aggregate(dt, eo, world, dev)
         e2e = {"value": eo / dt / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 8 * hin.numel(),
                "d2h_bytes_per_step": 8 * (eo // args.e2e_steps if world == 1 else int(eo / world) // args.e2e_steps),
                "steps": args.e2e_steps, "ms_per_step": 1000 * dt / args.e2e_steps}
