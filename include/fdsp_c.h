@@ -262,6 +262,42 @@ int fdsp_polar_apply(fdsp_polar *h, const fdsp_cf32 *d_in, uint64_t n_in, float 
 int fdsp_polar_apply_host(fdsp_polar *h, const fdsp_cf32 *h_in, uint64_t n_in, float *h_out, uint64_t *n_out,
                           fdsp_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Streaming server: many channelizer streams (jobs) served concurrently on
+ * one GPU.  No counterpart in the reference, whose classes run one blocking
+ * apply per object.
+ *
+ *   - fdsp_server_open admits a stream (its channel set, input rate, largest
+ *     block length, fdsp_precision) when its device footprint fits the
+ *     remaining budget and fewer than max_active streams are open; otherwise
+ *     it returns FDSP_ERR_CAPACITY and the caller retries after a close.  The
+ *     stream's filter history, resampler phase and NCO counter stay on the
+ *     device between its blocks.
+ *   - fdsp_server_submit enqueues one block on the stream's own CUDA stream
+ *     (host->device copy, channelizer apply, device->host copies into h_out)
+ *     and returns a ticket at once; blocks of one stream run in order, blocks
+ *     of different streams overlap on the GPU.  Host buffers should be pinned
+ *     and must stay valid until the ticket completes.
+ *   - fdsp_server_poll reports a ticket once, when done: its output counts and
+ *     its latency (submit to completion of the last device->host copy).
+ *   - fdsp_server_stats: p50/p99/p999 block latency (ms), blocks and output
+ *     samples completed since the last reset, bytes reserved, open streams.
+ * A server is not thread safe: drive it from one host thread.
+ * ---------------------------------------------------------------------- */
+typedef struct fdsp_server fdsp_server;
+
+int fdsp_server_create(uint64_t budget_bytes, uint32_t max_active, fdsp_server **out);
+int fdsp_server_destroy(fdsp_server *s);
+int fdsp_server_open(fdsp_server *s, uint32_t input_sample_rate, const fdsp_channel_cfg *channels,
+                     uint32_t num_channels, uint64_t max_block, int precision, uint32_t *stream_id);
+int fdsp_server_submit(fdsp_server *s, uint32_t stream_id, const fdsp_cf32 *h_in, uint64_t n_in,
+                       fdsp_cf32 *const *h_out, const uint64_t *out_cap, uint64_t *ticket);
+int fdsp_server_poll(fdsp_server *s, uint64_t ticket, int *done, uint64_t *n_out, double *latency_ms);
+int fdsp_server_close(fdsp_server *s, uint32_t stream_id);
+int fdsp_server_stats(fdsp_server *s, double *p50_ms, double *p99_ms, double *p999_ms, uint64_t *blocks,
+                      uint64_t *outputs, uint64_t *used_bytes, uint32_t *active);
+int fdsp_server_reset_stats(fdsp_server *s);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -12,6 +12,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libfalcon_dsp_gb300.so")
 
 FDSP_OK = 0
+FDSP_ERR_CAPACITY = -5
 STATUS = {
     0: "FDSP_OK",
     -1: "FDSP_ERR_INVALID_ARG",
@@ -71,6 +72,14 @@ SIGNATURES = {
     "fdsp_channelizer_apply_host": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
     "fdsp_channelizer_kernel_launches": [_vp, _pu32],
     "fdsp_channelizer_tc_groups": [_vp, _pu32],
+    "fdsp_server_create": [_u64, _u32, _pp],
+    "fdsp_server_destroy": [_vp],
+    "fdsp_server_open": [_vp, _u32, _vp, _u32, _u64, C.c_int, _pu32],
+    "fdsp_server_submit": [_vp, _u32, _vp, _u64, _vp, _vp, _pu64],
+    "fdsp_server_poll": [_vp, _u64, C.POINTER(C.c_int), _pu64, _pdbl],
+    "fdsp_server_close": [_vp, _u32],
+    "fdsp_server_stats": [_vp, _pdbl, _pdbl, _pdbl, _pu64, _pu64, _pu64, _pu32],
+    "fdsp_server_reset_stats": [_vp],
     "fdsp_channelizer_autotune": [_vp, _u64, _vp],
     "fdsp_channelizer_num_groups": [_vp, _pu32],
     "fdsp_channelizer_group_info": [_vp, _u32, _pu32, _pu32, C.POINTER(C.c_int)],

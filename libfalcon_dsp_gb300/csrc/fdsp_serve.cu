@@ -1,0 +1,242 @@
+// Streaming channelizer server: many concurrent streams (jobs) on one GPU.
+//
+// Each admitted stream owns a channelizer (its filter history, resampler
+// phase and NCO counter stay on the device between blocks), a CUDA stream,
+// one device input buffer of its maximum block length and one device output
+// buffer per channel.  A submitted block is enqueued on the stream's CUDA
+// stream as host->device copy, channelizer apply and device->host copies,
+// followed by a host function that stamps the completion time; blocks of
+// different streams overlap on the GPU.  Streams are admitted while their
+// device footprint fits the server's memory budget and the active-stream
+// limit, so new work starts as soon as earlier streams close.
+//
+// The reference has no server; its channelizer classes are one blocking
+// apply() per object (hdr/transform/falcon_dsp_multi_rate_channelizer_cuda.h:113).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "fdsp_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Ticket {
+  uint32_t sid = 0;
+  Clock::time_point t_submit;
+  std::atomic<int64_t> t_done_ns{0};  // completion, ns since t_submit (set by the host function)
+  std::atomic<int> done{0};
+  bool reported = false;
+  std::vector<uint64_t> n_out;
+};
+
+struct ServeStream {
+  fdsp_channelizer* ch = nullptr;
+  cudaStream_t cs = nullptr;
+  float2* d_in = nullptr;
+  std::vector<float2*> d_out;
+  std::vector<uint64_t> cap;
+  uint64_t max_block = 0;
+  uint64_t footprint = 0;
+  uint32_t nch = 0;
+  std::vector<uint64_t> up, down;
+};
+
+void CUDART_CB on_block_done(void* p) {
+  Ticket* t = static_cast<Ticket*>(p);
+  const int64_t ns = std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t->t_submit).count();
+  t->t_done_ns.store(ns > 0 ? ns : 1, std::memory_order_relaxed);
+  t->done.store(1, std::memory_order_release);
+}
+
+void free_stream(ServeStream& s) {
+  if (s.cs) cudaStreamSynchronize(s.cs);
+  if (s.ch) fdsp_channelizer_destroy(s.ch);
+  if (s.d_in) cudaFree(s.d_in);
+  for (auto p : s.d_out)
+    if (p) cudaFree(p);
+  if (s.cs) cudaStreamDestroy(s.cs);
+  s = ServeStream();
+}
+
+}  // namespace
+
+struct fdsp_server {
+  uint64_t budget = 0, used = 0;
+  uint32_t max_active = 0;
+  uint32_t next_sid = 1;
+  uint64_t next_ticket = 1;
+  std::map<uint32_t, ServeStream> streams;
+  std::map<uint64_t, std::unique_ptr<Ticket>> tickets;
+  std::vector<double> lat_ms;
+  uint64_t outputs = 0;
+  std::mutex mu;
+};
+
+using namespace fdsp;
+
+// Device bytes a stream holds: input and output buffers, the channelizer's
+// taps, history and (tensor-core precisions) its split-input scratch.
+static uint64_t stream_footprint(const fdsp_channel_cfg* ch, uint32_t nch, uint64_t max_block, int precision) {
+  uint64_t b = 8 * max_block + (1u << 20);
+  uint64_t hist = 0;
+  for (uint32_t c = 0; c < nch; ++c) {
+    b += 8 * ((max_block * ch[c].up_rate + ch[c].down_rate - 1) / ch[c].down_rate + 2);
+    b += 16ull * ch[c].num_coeffs + 64ull * ch[c].num_coeffs;  // FP32 and tensor-core tap tables
+    hist = std::max<uint64_t>(hist, ch[c].num_coeffs / std::max(1u, ch[c].up_rate) + 1);
+  }
+  b += 16 * hist;
+  if (precision != FDSP_PRECISION_FP32) b += 8 * (max_block + hist);
+  return b;
+}
+
+extern "C" int fdsp_server_create(uint64_t budget_bytes, uint32_t max_active, fdsp_server** out) {
+  if (!out || budget_bytes == 0 || max_active == 0) return FDSP_ERR_INVALID_ARG;
+  fdsp_server* s = new (std::nothrow) fdsp_server();
+  if (!s) return FDSP_ERR_ALLOC;
+  s->budget = budget_bytes;
+  s->max_active = max_active;
+  *out = s;
+  return FDSP_OK;
+}
+
+extern "C" int fdsp_server_destroy(fdsp_server* s) {
+  if (!s) return FDSP_ERR_NOT_INITIALIZED;
+  for (auto& kv : s->streams) free_stream(kv.second);
+  delete s;
+  return FDSP_OK;
+}
+
+extern "C" int fdsp_server_open(fdsp_server* s, uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch,
+                                uint64_t max_block, int precision, uint32_t* sid) {
+  if (!s) return FDSP_ERR_NOT_INITIALIZED;
+  if (!ch || nch == 0 || max_block == 0 || !sid) return FDSP_ERR_INVALID_ARG;
+  const uint64_t fp = stream_footprint(ch, nch, max_block, precision);
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->streams.size() >= s->max_active || s->used + fp > s->budget) return FDSP_ERR_CAPACITY;
+    s->used += fp;  // reserved while the stream is set up
+  }
+  ServeStream st;
+  st.max_block = max_block;
+  st.footprint = fp;
+  st.nch = nch;
+  int rc = fdsp_channelizer_create(fs, ch, nch, &st.ch);
+  if (rc == FDSP_OK && precision != FDSP_PRECISION_FP32) rc = fdsp_channelizer_set_precision(st.ch, precision);
+  if (rc == FDSP_OK) rc = cuda_status(cudaStreamCreateWithFlags(&st.cs, cudaStreamNonBlocking));
+  if (rc == FDSP_OK) rc = cuda_status(cudaMalloc(&st.d_in, 8 * max_block));
+  st.d_out.assign(nch, nullptr);
+  st.cap.assign(nch, 0);
+  for (uint32_t c = 0; c < nch && rc == FDSP_OK; ++c) {
+    st.cap[c] = (max_block * ch[c].up_rate + ch[c].down_rate - 1) / ch[c].down_rate + 2;
+    rc = cuda_status(cudaMalloc(&st.d_out[c], 8 * st.cap[c]));
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (rc != FDSP_OK) {
+    free_stream(st);
+    s->used -= fp;
+    return rc;
+  }
+  const uint32_t id = s->next_sid++;
+  s->streams.emplace(id, std::move(st));
+  *sid = id;
+  return FDSP_OK;
+}
+
+extern "C" int fdsp_server_submit(fdsp_server* s, uint32_t sid, const fdsp_cf32* h_in, uint64_t n_in,
+                                  fdsp_cf32* const* h_out, const uint64_t* out_cap, uint64_t* ticket) {
+  if (!s) return FDSP_ERR_NOT_INITIALIZED;
+  if (!h_in || n_in == 0 || !h_out || !ticket) return FDSP_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->streams.find(sid);
+  if (it == s->streams.end()) return FDSP_ERR_INVALID_ARG;
+  ServeStream& st = it->second;
+  if (n_in > st.max_block) return FDSP_ERR_CAPACITY;
+  std::unique_ptr<Ticket> t(new (std::nothrow) Ticket());
+  if (!t) return FDSP_ERR_ALLOC;
+  t->sid = sid;
+  t->n_out.assign(st.nch, 0);
+  t->t_submit = Clock::now();
+  int rc = cuda_status(cudaMemcpyAsync(st.d_in, h_in, 8 * n_in, cudaMemcpyHostToDevice, st.cs));
+  if (rc == FDSP_OK)
+    rc = fdsp_channelizer_apply(st.ch, reinterpret_cast<const fdsp_cf32*>(st.d_in), n_in,
+                                reinterpret_cast<fdsp_cf32* const*>(st.d_out.data()), st.cap.data(), t->n_out.data(),
+                                (fdsp_stream_t)st.cs);
+  for (uint32_t c = 0; c < st.nch && rc == FDSP_OK; ++c) {
+    if (out_cap && out_cap[c] < t->n_out[c]) rc = FDSP_ERR_CAPACITY;
+    if (rc == FDSP_OK && t->n_out[c])
+      rc = cuda_status(cudaMemcpyAsync(h_out[c], st.d_out[c], 8 * t->n_out[c], cudaMemcpyDeviceToHost, st.cs));
+  }
+  if (rc == FDSP_OK) rc = cuda_status(cudaLaunchHostFunc(st.cs, on_block_done, t.get()));
+  if (rc != FDSP_OK) {
+    cudaStreamSynchronize(st.cs);  // nothing of this ticket may still reference it
+    return rc;
+  }
+  const uint64_t id = s->next_ticket++;
+  s->tickets.emplace(id, std::move(t));
+  *ticket = id;
+  return FDSP_OK;
+}
+
+extern "C" int fdsp_server_poll(fdsp_server* s, uint64_t ticket, int* done, uint64_t* n_out, double* latency_ms) {
+  if (!s) return FDSP_ERR_NOT_INITIALIZED;
+  if (!done) return FDSP_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return FDSP_ERR_INVALID_ARG;
+  Ticket& t = *it->second;
+  *done = t.done.load(std::memory_order_acquire);
+  if (!*done) return FDSP_OK;
+  const double ms = (double)t.t_done_ns.load(std::memory_order_relaxed) / 1e6;
+  if (latency_ms) *latency_ms = ms;
+  if (n_out) std::copy(t.n_out.begin(), t.n_out.end(), n_out);
+  uint64_t tot = 0;
+  for (auto v : t.n_out) tot += v;
+  s->lat_ms.push_back(ms);
+  s->outputs += tot;
+  s->tickets.erase(it);  // a completed ticket is reported once
+  return FDSP_OK;
+}
+
+extern "C" int fdsp_server_close(fdsp_server* s, uint32_t sid) {
+  if (!s) return FDSP_ERR_NOT_INITIALIZED;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->streams.find(sid);
+  if (it == s->streams.end()) return FDSP_ERR_INVALID_ARG;
+  s->used -= it->second.footprint;
+  free_stream(it->second);  // waits for the stream's blocks
+  s->streams.erase(it);
+  return FDSP_OK;
+}
+
+extern "C" int fdsp_server_stats(fdsp_server* s, double* p50_ms, double* p99_ms, double* p999_ms, uint64_t* blocks,
+                                 uint64_t* outputs, uint64_t* used_bytes, uint32_t* active) {
+  if (!s) return FDSP_ERR_NOT_INITIALIZED;
+  std::lock_guard<std::mutex> lk(s->mu);
+  std::vector<double> v = s->lat_ms;
+  std::sort(v.begin(), v.end());
+  auto q = [&](double p) { return v.empty() ? 0.0 : v[std::min(v.size() - 1, (size_t)(p * (double)(v.size() - 1) + 0.5))]; };
+  if (p50_ms) *p50_ms = q(0.5);
+  if (p99_ms) *p99_ms = q(0.99);
+  if (p999_ms) *p999_ms = q(0.999);
+  if (blocks) *blocks = v.size();
+  if (outputs) *outputs = s->outputs;
+  if (used_bytes) *used_bytes = s->used;
+  if (active) *active = (uint32_t)s->streams.size();
+  return FDSP_OK;
+}
+
+extern "C" int fdsp_server_reset_stats(fdsp_server* s) {
+  if (!s) return FDSP_ERR_NOT_INITIALIZED;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->lat_ms.clear();
+  s->outputs = 0;
+  return FDSP_OK;
+}
