@@ -279,7 +279,8 @@ int fdsp_polar_apply_host(fdsp_polar *h, const fdsp_cf32 *h_in, uint64_t n_in, f
  *     of different streams overlap on the GPU.  Host buffers should be pinned
  *     and must stay valid until the ticket completes.
  *   - fdsp_server_poll reports a ticket once, when done: its output counts and
- *     its latency (submit to completion of the last device->host copy).
+ *     its latency (submit to completion of the last device->host copy);
+ *     fdsp_server_wait_any hands out completed tickets in completion order.
  *   - fdsp_server_stats: p50/p99/p999 block latency (ms), blocks and output
  *     samples completed since the last reset, bytes reserved, open streams.
  * A server is not thread safe: drive it from one host thread.
@@ -293,6 +294,9 @@ int fdsp_server_open(fdsp_server *s, uint32_t input_sample_rate, const fdsp_chan
 int fdsp_server_submit(fdsp_server *s, uint32_t stream_id, const fdsp_cf32 *h_in, uint64_t n_in,
                        fdsp_cf32 *const *h_out, const uint64_t *out_cap, uint64_t *ticket);
 int fdsp_server_poll(fdsp_server *s, uint64_t ticket, int *done, uint64_t *n_out, double *latency_ms);
+/* Next completed ticket in completion order (waits up to timeout_us; *ticket
+ * = 0 when none completed); then fdsp_server_poll reports it. */
+int fdsp_server_wait_any(fdsp_server *s, uint32_t timeout_us, uint64_t *ticket);
 int fdsp_server_close(fdsp_server *s, uint32_t stream_id);
 int fdsp_server_stats(fdsp_server *s, double *p50_ms, double *p99_ms, double *p999_ms, uint64_t *blocks,
                       uint64_t *outputs, uint64_t *used_bytes, uint32_t *active);

@@ -78,6 +78,7 @@ SIGNATURES = {
     "fdsp_server_submit": [_vp, _u32, _vp, _u64, _vp, _vp, _pu64],
     "fdsp_server_poll": [_vp, _u64, C.POINTER(C.c_int), _pu64, _pdbl],
     "fdsp_server_close": [_vp, _u32],
+    "fdsp_server_wait_any": [_vp, _u32, _pu64],
     "fdsp_server_stats": [_vp, _pdbl, _pdbl, _pdbl, _pu64, _pu64, _pu64, _pu32],
     "fdsp_server_reset_stats": [_vp],
     "fdsp_channelizer_autotune": [_vp, _u64, _vp],

@@ -15,7 +15,9 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -28,8 +30,16 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+struct DoneQueue {  // tickets completed on the GPU, in completion order
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<uint64_t> ids;
+};
+
 struct Ticket {
   uint32_t sid = 0;
+  uint64_t id = 0;
+  DoneQueue* q = nullptr;
   Clock::time_point t_submit;
   std::atomic<int64_t> t_done_ns{0};  // completion, ns since t_submit (set by the host function)
   std::atomic<int> done{0};
@@ -54,6 +64,11 @@ void CUDART_CB on_block_done(void* p) {
   const int64_t ns = std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t->t_submit).count();
   t->t_done_ns.store(ns > 0 ? ns : 1, std::memory_order_relaxed);
   t->done.store(1, std::memory_order_release);
+  {
+    std::lock_guard<std::mutex> lk(t->q->mu);
+    t->q->ids.push_back(t->id);
+  }
+  t->q->cv.notify_one();
 }
 
 void free_stream(ServeStream& s) {
@@ -78,6 +93,7 @@ struct fdsp_server {
   std::vector<double> lat_ms;
   uint64_t outputs = 0;
   std::mutex mu;
+  DoneQueue done;
 };
 
 using namespace fdsp;
@@ -162,6 +178,8 @@ extern "C" int fdsp_server_submit(fdsp_server* s, uint32_t sid, const fdsp_cf32*
   std::unique_ptr<Ticket> t(new (std::nothrow) Ticket());
   if (!t) return FDSP_ERR_ALLOC;
   t->sid = sid;
+  t->id = s->next_ticket;
+  t->q = &s->done;
   t->n_out.assign(st.nch, 0);
   t->t_submit = Clock::now();
   int rc = cuda_status(cudaMemcpyAsync(st.d_in, h_in, 8 * n_in, cudaMemcpyHostToDevice, st.cs));
@@ -202,6 +220,21 @@ extern "C" int fdsp_server_poll(fdsp_server* s, uint64_t ticket, int* done, uint
   s->lat_ms.push_back(ms);
   s->outputs += tot;
   s->tickets.erase(it);  // a completed ticket is reported once
+  return FDSP_OK;
+}
+
+extern "C" int fdsp_server_wait_any(fdsp_server* s, uint32_t timeout_us, uint64_t* ticket) {
+  if (!s) return FDSP_ERR_NOT_INITIALIZED;
+  if (!ticket) return FDSP_ERR_INVALID_ARG;
+  std::unique_lock<std::mutex> lk(s->done.mu);
+  if (s->done.ids.empty() && timeout_us)
+    s->done.cv.wait_for(lk, std::chrono::microseconds(timeout_us), [&] { return !s->done.ids.empty(); });
+  if (s->done.ids.empty()) {
+    *ticket = 0;
+    return FDSP_OK;
+  }
+  *ticket = s->done.ids.front();
+  s->done.ids.pop_front();
   return FDSP_OK;
 }
 

@@ -80,6 +80,12 @@ class ChannelizerServer:
         _capi.call("fdsp_server_poll", self._h, int(ticket), C.byref(done), n_out, C.byref(lat))
         return bool(done.value), list(n_out), lat.value
 
+    def wait_any(self, timeout_us: int = 1000) -> int:
+        """Next completed ticket (0 when none completed within the timeout)."""
+        t = C.c_uint64()
+        _capi.call("fdsp_server_wait_any", self._h, int(timeout_us), C.byref(t))
+        return t.value
+
     def close(self, sid: int) -> None:
         _capi.call("fdsp_server_close", self._h, int(sid))
 
@@ -96,6 +102,16 @@ class ChannelizerServer:
         _capi.call("fdsp_server_reset_stats", self._h)
 
 
+_TAPS: dict = {}
+
+
+def _taps(u: int, d: int, tpp: int) -> np.ndarray:
+    key = (u, d, tpp)
+    if key not in _TAPS:
+        _TAPS[key] = kaiser_lowpass(u, d, tpp).astype(np.complex64)
+    return _TAPS[key]
+
+
 def random_job(rng: np.random.Generator, max_channels: int = 64, block_range=(4096, 1 << 20),
                blocks_range=(10, 200)) -> dict:
     """One streaming job of the serving workload (parameters as documented above)."""
@@ -110,7 +126,7 @@ def random_job(rng: np.random.Generator, max_channels: int = 64, block_range=(40
         u, d = u // g, d // g
         tpp = int(rng.integers(12, 65))
         chans.append({"freq_shift_in_hz": int(rng.uniform(-0.45, 0.45) * fs), "up_rate": u, "down_rate": d,
-                      "coeffs": kaiser_lowpass(u, d, tpp).astype(np.complex64)})
+                      "coeffs": _taps(u, d, tpp)})
     return {"fs": fs, "channels": chans, "block": int(rng.integers(block_range[0], block_range[1] + 1)),
             "blocks": int(rng.integers(blocks_range[0], blocks_range[1] + 1))}
 
@@ -143,23 +159,27 @@ def run_serving(duration_s: float = 5.0, rate_hz: float = 2000.0, seed: int = 4,
     next_arrival = t0 + rng.exponential(1.0 / rate_hz)
     arrived = admitted = completed_jobs = 0
     wait_admit = []
+    head = None
+    by_ticket = {}
     while True:
         now = time.perf_counter()
         while next_arrival <= now and next_arrival - t0 < duration_s:
-            job = random_job(rng, block_range=block_range)
-            if max_blocks_per_job:
-                job["blocks"] = min(job["blocks"], max_blocks_per_job)
-            job["t_arrive"] = next_arrival
-            pending.append(job)
+            pending.append(next_arrival)  # the job itself is drawn when it is admitted
             arrived += 1
             next_arrival += rng.exponential(1.0 / rate_hz)
         # admission: as many waiting jobs as memory and slots allow
         while pending and free_arenas:
-            job = pending[0]
+            if head is None:
+                head = random_job(rng, block_range=block_range)
+                if max_blocks_per_job:
+                    head["blocks"] = min(head["blocks"], max_blocks_per_job)
+                head["t_arrive"] = pending[0]
+            job = head
             sid = srv.open(job["fs"], job["channels"], job["block"], precision)
             if sid is None:
                 break
             pending.popleft()
+            head = None
             arena = free_arenas.popleft()
             caps = _out_caps(job)
             ptrs, off = [], 0
@@ -169,24 +189,28 @@ def run_serving(duration_s: float = 5.0, rate_hz: float = 2000.0, seed: int = 4,
             job.update(sid=sid, arena=arena, caps=caps, ptrs=ptrs, left=job["blocks"],
                        src=in_base + 8 * int(rng.integers(0, pool_n - job["block"])))
             wait_admit.append(time.perf_counter() - job["t_arrive"])
-            job["ticket"] = srv.submit(sid, job["src"], job["block"], ptrs, caps)
+            t = srv.submit(sid, job["src"], job["block"], ptrs, caps)
+            by_ticket[t] = sid
             job["left"] -= 1
             active[sid] = job
             admitted += 1
-        # progress: next block of every job whose previous block completed
-        for sid in list(active):
+        # progress: the next block of each job whose previous block completed
+        # (completed tickets come from the server's completion queue)
+        t = srv.wait_any(200 if active else 0)
+        while t:
+            sid = by_ticket.pop(t)
             job = active[sid]
-            done, _, _ = srv.poll(job["ticket"], len(job["channels"]))
-            if not done:
-                continue
+            srv.poll(t, len(job["channels"]))
             if job["left"] > 0:
-                job["ticket"] = srv.submit(sid, job["src"], job["block"], job["ptrs"], job["caps"])
+                t2 = srv.submit(sid, job["src"], job["block"], job["ptrs"], job["caps"])
+                by_ticket[t2] = sid
                 job["left"] -= 1
             else:
                 srv.close(sid)
                 free_arenas.append(job["arena"])
                 del active[sid]
                 completed_jobs += 1
+            t = srv.wait_any(0)
         if now - t0 >= duration_s and not active:
             break
         if now - t0 >= duration_s and pending:
