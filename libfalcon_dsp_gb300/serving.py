@@ -64,12 +64,19 @@ class ChannelizerServer:
         _capi.check("fdsp_server_open", st)
         return sid.value
 
-    def submit(self, sid: int, in_ptr: int, n_in: int, out_ptrs, out_caps) -> int:
-        t = C.c_uint64()
+    @staticmethod
+    def out_args(out_ptrs, out_caps):
+        """ctypes arrays of output pointers and capacities, built once per job."""
         n = len(out_ptrs)
-        optr = (C.c_void_p * n)(*out_ptrs)
-        caps = (C.c_uint64 * n)(*out_caps)
-        _capi.call("fdsp_server_submit", self._h, int(sid), C.c_void_p(in_ptr), int(n_in), optr, caps, C.byref(t))
+        return (C.c_void_p * n)(*out_ptrs), (C.c_uint64 * n)(*out_caps)
+
+    def submit(self, sid: int, in_ptr: int, n_in: int, out_ptrs, out_caps) -> int:
+        if not isinstance(out_ptrs, C.Array):
+            out_ptrs, out_caps = self.out_args(out_ptrs, out_caps)
+        t = C.c_uint64()
+        st = _capi.lib().fdsp_server_submit(self._h, sid, in_ptr, n_in, out_ptrs, out_caps, C.byref(t))
+        if st:
+            _capi.check("fdsp_server_submit", st)
         return t.value
 
     def poll(self, ticket: int, nch: int):
@@ -186,10 +193,11 @@ def run_serving(duration_s: float = 5.0, rate_hz: float = 2000.0, seed: int = 4,
             for c in caps:
                 ptrs.append(arena.data_ptr() + off)
                 off += 8 * c
-            job.update(sid=sid, arena=arena, caps=caps, ptrs=ptrs, left=job["blocks"],
+            optr, ocap = ChannelizerServer.out_args(ptrs, caps)
+            job.update(sid=sid, arena=arena, caps=ocap, ptrs=optr, left=job["blocks"],
                        src=in_base + 8 * int(rng.integers(0, pool_n - job["block"])))
             wait_admit.append(time.perf_counter() - job["t_arrive"])
-            t = srv.submit(sid, job["src"], job["block"], ptrs, caps)
+            t = srv.submit(sid, job["src"], job["block"], optr, ocap)
             by_ticket[t] = sid
             job["left"] -= 1
             active[sid] = job
