@@ -168,6 +168,16 @@ class MultiRateChannelizerCuda(_Handle):
         _capi.call("fdsp_channelizer_autotune", self._h, int(n_in), C.c_void_p(s))
         return self.group_info()
 
+    def set_graph(self, enable: bool = True) -> None:
+        """Replay every later apply's launches as one CUDA graph (applies on
+        the legacy default stream launch directly)."""
+        _capi.call("fdsp_channelizer_set_graph", self._h, 1 if enable else 0)
+
+    def graph_replays(self) -> int:
+        v = C.c_uint32()
+        _capi.call("fdsp_channelizer_graph_replays", self._h, C.byref(v))
+        return v.value
+
     def group_info(self) -> list[dict]:
         n = C.c_uint32()
         _capi.call("fdsp_channelizer_num_groups", self._h, C.byref(n))

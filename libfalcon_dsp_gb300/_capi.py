@@ -83,6 +83,8 @@ SIGNATURES = {
     "fdsp_server_reset_stats": [_vp],
     "fdsp_channelizer_autotune": [_vp, _u64, _vp],
     "fdsp_channelizer_num_groups": [_vp, _pu32],
+    "fdsp_channelizer_set_graph": [_vp, C.c_int],
+    "fdsp_channelizer_graph_replays": [_vp, _pu32],
     "fdsp_channelizer_group_info": [_vp, _u32, _pu32, _pu32, C.POINTER(C.c_int)],
     "fdsp_channelizer_set_precision": [_vp, C.c_int],
     "fdsp_resampler_create": [_u32, _u32, _vp, _u32, _pp],

@@ -252,6 +252,19 @@ int fdsp_channelizer_autotune(fdsp_channelizer* h, uint64_t n_in, fdsp_stream_t 
   return h->eng.autotune(n_in, (cudaStream_t)stream);
 }
 
+int fdsp_channelizer_set_graph(fdsp_channelizer* h, int enable) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  h->eng.set_graph(enable != 0);
+  return FDSP_OK;
+}
+
+int fdsp_channelizer_graph_replays(const fdsp_channelizer* h, uint32_t* replays) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!replays) return FDSP_ERR_INVALID_ARG;
+  *replays = (uint32_t)h->eng.graph_replays();
+  return FDSP_OK;
+}
+
 int fdsp_channelizer_num_groups(const fdsp_channelizer* h, uint32_t* n) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
   if (!n) return FDSP_ERR_INVALID_ARG;

@@ -299,6 +299,7 @@ NcoConst make_nco(uint32_t fs, int32_t f) {
 }
 
 PolyEngine::~PolyEngine() {
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
   free_tc();
   for (auto& b : batches_) {
     if (b.d_taps) cudaFree(b.d_taps);
@@ -514,6 +515,15 @@ int PolyEngine::set_precision(int mode) {
   if (st != FDSP_OK) return st;
   precision_ = mode;
   return FDSP_OK;
+}
+
+void PolyEngine::set_graph(bool on) {
+  use_graph_ = on;
+  graph_replays_ = 0;
+  if (!on && graph_exec_) {
+    cudaGraphExecDestroy(graph_exec_);
+    graph_exec_ = nullptr;
+  }
 }
 
 bool PolyEngine::use_tc_for(int eg) const {
@@ -765,12 +775,46 @@ int PolyEngine::apply(const float2* d_in, uint64_t n, float2* const* out, const 
     if (cap && cap[c] < M) return FDSP_ERR_CAPACITY;
   }
   if (n == 0) return FDSP_OK;
+  cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+  const bool graph = use_graph_ && stream != nullptr && cudaStreamIsCapturing(stream, &capturing) == cudaSuccess &&
+                     capturing == cudaStreamCaptureStatusNone;
+  if (graph) {
+    const cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
   int st;
   switch (nb_) {
     case 1: st = launch<1>(d_in, n, out, stream); break;
     case 2: st = launch<2>(d_in, n, out, stream); break;
     case 4: st = launch<4>(d_in, n, out, stream); break;
     default: st = launch<8>(d_in, n, out, stream); break;
+  }
+  if (graph) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (st == FDSP_OK && e != cudaSuccess) st = cuda_status(e);
+    if (st == FDSP_OK && graph_exec_) {
+      // same launch sequence shape: only kernel parameters and grids change
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(graph_exec_, g, &info) != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(graph_exec_);
+        graph_exec_ = nullptr;
+      }
+    }
+    if (st == FDSP_OK && !graph_exec_) {
+      e = cudaGraphInstantiate(&graph_exec_, g, 0);
+      if (e != cudaSuccess) {
+        graph_exec_ = nullptr;
+        st = cuda_status(e);
+      }
+    }
+    if (st == FDSP_OK) {
+      e = cudaGraphLaunch(graph_exec_, stream);
+      if (e != cudaSuccess) st = cuda_status(e);
+      else graph_replays_++;
+    }
+    if (g) cudaGraphDestroy(g);
   }
   if (st != FDSP_OK) return st;
   // advance the streaming state (polyphase_resampler.cc:303-312)

@@ -255,6 +255,12 @@ class PolyEngine {
   // tensor-core precision; keep the fastest per group.  Resets the stream.
   int autotune(uint64_t n, cudaStream_t stream);
   int num_groups() const { return (int)groups_.size(); }
+  // CUDA-graph replay of each apply's launch sequence (captured on the
+  // caller's stream, the instantiated graph updated in place while the
+  // sequence keeps its shape).  Applies on the legacy default stream, or on a
+  // stream the caller is capturing, launch directly.
+  void set_graph(bool on);
+  int graph_replays() const { return graph_replays_; }
   void group_info(int g, uint32_t* D, int* Qt, int* use_tc) const {
     *D = groups_[g].D;
     *Qt = groups_[g].Qt;
@@ -295,6 +301,9 @@ class PolyEngine {
   int launches_last_ = 0;
   int tc_groups_last_ = 0;
   int force_ = -1;                     // autotuning: -1 chosen forms, 0 all FP32, 1 all tensor cores
+  bool use_graph_ = false;
+  cudaGraphExec_t graph_exec_ = nullptr;
+  int graph_replays_ = 0;              // applies replayed as a graph since set_graph(true)
   bool use_tc_for(int eg) const;
   std::vector<cudaEvent_t> prof_ev_;   // autotuning: [2 g] / [2 g + 1] around group g
   std::vector<int> prof_hit_;          // group g launched in the timed apply
