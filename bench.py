@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--no-fp32-compare", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--serve-streams", type=int, default=8, help="concurrent streams the server admits")
     return ap.parse_args()
@@ -237,6 +238,8 @@ def run_ours(args) -> None:
     # per decimation group: FP32 tile height and tensor-core vs FP32 form,
     # timed on this workload's block size (resets the streaming state)
     tune = ch.autotune(x.numel()) if not args.no_autotune else ch.group_info()
+    # each step's launches replayed as one CUDA graph (updated in place)
+    ch.set_graph(not args.no_graph)
     nch = len(chans)
     stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
@@ -386,6 +389,7 @@ def run_ours(args) -> None:
                                 "bf16x3": "tensor cores (tcgen05), BF16 (hi+lo)(hi+lo), FP32 accumulate"}[args.precision],
                        "autotune": [{"down": t["down_rate"], "tile_rows": t["tile_rows"], "tc": t["tensor_core"]}
                                     for t in tune],
+                       "cuda_graph": not args.no_graph, "graph_replays": ch.graph_replays(),
                        "l2": "no flush: each step reads 512 MiB and writes ~9.6 GB, far above the 129 MB L2",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_step * args.steps,
