@@ -77,7 +77,7 @@ struct SlotMeta {
   uint32_t Tm1;           // taps - 1 (0x7fffffff: general, every output exact)
   int32_t U, r;           // output m = r + U j
   int32_t J;              // rows with an output (0: padding slot)
-  uint32_t short_r;       // 1: R <= 127 D + T, the row counter is reduced in full
+  uint32_t pad0_;
   uint64_t fastmod;       // ceil(2^64 / R)
   int32_t delta;          // window end of row 0
   int32_t T;
@@ -240,8 +240,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
               // once when 127 D + T < R, else reduced with the fast modulo;
               // R >= 2^31 ("general") takes the exact path for every output
               const bool general = nc.enabled && nc.rollover >= 0x80000000u;
-              sm.short_r =
-                  (nc.enabled && !general && (uint64_t)nc.rollover <= 127ull * D + (uint64_t)W.T) ? 1u : 0u;
               sm.fastmod = nc.fastmod;
               sm.om_lo = nc.enabled && !general ? (uint32_t)nc.omega64 : 0u;
               sm.om_hi = nc.enabled && !general ? (uint32_t)(nc.omega64 >> 32) : 0u;
@@ -487,13 +485,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
           const TcSlotHot sh = hot[e];
           const uint32_t P0 = __shfl_sync(0xffffffffu, si < 32 ? p0a : p0b, si & 31);
           const uint32_t R = sh.R;
-          uint32_t pc = P0 + rowD;
-          if (sh.ur >> 31) {  // short rollover (uniform over the warp): full reduction
-            const uint64_t fm = meta[si].fastmod;
-            pc = (uint32_t)__umul64hi(fm * (uint64_t)pc, (uint64_t)R);
-          } else {
-            pc = pc >= R ? pc - R : pc;
-          }
+          // (P0 + row D) mod R without a branch: quotient estimate from 1/R
+          // in FP32 (off by at most one for these magnitudes), then one
+          // correction each way
+          const uint32_t a = P0 + rowD;
+          const uint32_t qe = __float2uint_rz(__uint2float_rz(a) * sh.invR);
+          int64_t rem = (int64_t)a - (int64_t)qe * R;  // in [-R, 2R)
+          rem = rem < 0 ? rem + R : rem;
+          rem = rem >= (int64_t)R ? rem - R : rem;
+          const uint32_t pc = (uint32_t)rem;
           const bool okr = pc + sh.Tm1 < R;
           // bits 32..63 of pc * omega64: the phase in 2^-32 turns
           const uint32_t turns = __umulhi(pc, sh.om_lo) + pc * sh.om_hi;
@@ -938,6 +938,7 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
       for (int sI = 0; sI < M.N / 2; ++sI) {
         TcSlotHot& h = L.slot[nslot++];
         h.R = 0x7fffffffu;
+        h.invR = 1.0f / (float)h.R;
         for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
           const TcWorkSet& W = L.ws[wi];
           const int i = sI - 4 * W.cg0;
@@ -947,15 +948,15 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
             const int c = w.ch->chans[i];
             const NcoConst& nc = chans_[c].nco;
             const bool general = nc.enabled && nc.rollover >= 0x80000000u;
-            const bool shortr = nc.enabled && !general && (uint64_t)nc.rollover <= 127ull * D + (uint64_t)W.T;
             h.om_lo = nc.enabled && !general ? (uint32_t)nc.omega64 : 0u;
             h.om_hi = nc.enabled && !general ? (uint32_t)(nc.omega64 >> 32) : 0u;
             h.out_lo = (uint32_t)(uintptr_t)out[c];
             h.out_hi = (uint32_t)((uintptr_t)out[c] >> 32);
             h.R = nc.enabled && !general ? nc.rollover : 0x7fffffffu;
             h.Tm1 = general ? 0x7fffffffu : (uint32_t)(W.T - 1);
-            h.ur = (uint32_t)W.U | ((uint32_t)W.r << 16) | (shortr ? 0x80000000u : 0u);
+            h.ur = (uint32_t)W.U | ((uint32_t)W.r << 16);
             h.J = W.J;
+            h.invR = 1.0f / (float)h.R;
           }
           break;
         }

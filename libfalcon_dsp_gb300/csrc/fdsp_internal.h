@@ -132,8 +132,10 @@ struct TcSlotHot {
   uint32_t out_lo, out_hi;// output base of the channel
   uint32_t R;             // counter rollover (0x7fffffff: no shift, or exact path)
   uint32_t Tm1;           // taps - 1 (0x7fffffff: every output on the exact path)
-  uint32_t ur;            // U | r << 16 | short rollover << 31 (output m = r + U j)
+  uint32_t ur;            // U | r << 16 (output m = r + U j)
   int32_t J;              // rows with an output (0: padding slot)
+  float invR;             // 1 / R (row counter reduction)
+  uint32_t pad_[3];
 };
 
 struct TcLaunch {
