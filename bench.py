@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-other-configs", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--serve-streams", type=int, default=8, help="concurrent streams the server admits")
     return ap.parse_args()
@@ -166,6 +167,80 @@ def cpu_channelizer_rate(fs, chans, x, threads, use_reference: bool) -> tuple[fl
         tot = sum(ex.map(work, objs))
     dt = time.perf_counter() - t0
     return tot / dt / 1e6, kind, threads
+
+
+def _time_device(fn, reps: int = 5, warm: int = 3):
+    """Median ms of fn() over reps runs, CUDA events on the current stream."""
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts)), out
+
+
+def other_configs(dev) -> dict:
+    import torch
+
+    import libfalcon_dsp_gb300 as F
+    from libfalcon_dsp_gb300.workloads import audio_snr_db, channelizer_8ch, fm_chain, resampler_1ch
+    res = {}
+    # single-channel resampler 48 kHz -> 44.1 kHz, 2^20 samples, 3528 taps
+    x, up, down, h = resampler_1ch(1 << 20, 2024, device=dev)
+    rs = F.PolyphaseResamplerCuda(up, down, h)
+    out = torch.empty(rs.out_count(x.numel()) + 2, dtype=torch.complex64, device=dev)
+
+    def c1():
+        rs.reset_state()
+        return rs.apply(x, out=out).numel()
+    ms, n_out = _time_device(c1)
+    res["resampler_147_160"] = {"n_in": x.numel(), "n_out": n_out, "ms": round(ms, 4),
+                                "value": round(n_out / ms / 1e3, 1), "unit": "Msamples/s"}
+    # 8-channel channelizer, 2^24 samples streamed in 2^16-sample blocks
+    x, fs, chans = channelizer_8ch(1 << 24, 2025, device=dev)
+    ch = F.MultiRateChannelizerCuda(fs, chans)
+    blk = 1 << 16
+    outs = [torch.empty(c + 2, dtype=torch.complex64, device=dev) for c in ch.out_count(blk)]
+    s = torch.cuda.Stream(device=dev)
+    ch.set_graph(True)
+
+    def c2():
+        ch.reset_state()
+        tot = 0
+        with torch.cuda.stream(s):
+            for b in range(x.numel() // blk):
+                tot += sum(y.numel() for y in ch.apply(x[b * blk:(b + 1) * blk], out=outs))
+        torch.cuda.current_stream().wait_stream(s)
+        return tot
+    ms, n_out = _time_device(c2, reps=3, warm=1)
+    res["channelizer_8ch_blocks_2p16"] = {"n_in": x.numel(), "blocks": x.numel() // blk, "n_out": n_out,
+                                          "ms": round(ms, 3), "value": round(n_out / ms / 1e3, 1),
+                                          "unit": "Msamples/s", "cuda_graph": True}
+    # FIR 4095 taps / decimate 10 / polar discriminator, 2^26 samples
+    x, fs, h, tones = fm_chain(1 << 26, 2027, device=dev)
+    rs = F.PolyphaseResamplerCuda(1, 10, h)
+    pd = F.PolarDiscriminatorCuda()
+    y = torch.empty(rs.out_count(x.numel()) + 2, dtype=torch.complex64, device=dev)
+    a = torch.empty(y.numel() + 2, dtype=torch.float32, device=dev)
+
+    def c5():
+        rs.reset_state()
+        pd.reset_state()
+        yy = rs.apply(x, out=y)
+        return pd.apply(yy, out=a).numel()
+    ms, n_aud = _time_device(c5, reps=3, warm=1)
+    snr = audio_snr_db(a[:n_aud].cpu().numpy(), fs / 10, tones)
+    res["fir4095_dec10_fm"] = {"n_in": x.numel(), "n_audio": n_aud, "ms": round(ms, 3),
+                               "value": round(x.numel() / ms / 1e3, 1), "unit": "input Msamples/s",
+                               "audio_snr_db": round(snr, 2), "fir_gflops": round(4 * 4095 * (n_aud + 1) / ms / 1e6, 1)}
+    return res
 
 
 def replica_aggregate(t, units, world: int, dev):
@@ -351,6 +426,14 @@ def run_ours(args) -> None:
                "d2h_bytes_per_step": 8 * (eo // args.e2e_steps if world == 1 else int(eo / world) // args.e2e_steps),
                "steps": args.e2e_steps, "ms_per_step": 1000 * dt / args.e2e_steps}
 
+    # the other workloads of the path, each timed on the device (inputs
+    # resident, CUDA events, after warm-up): single-channel 147/160 resampler,
+    # 8-channel streaming channelizer in 2^16-sample blocks, and the 4095-tap
+    # FIR / decimate-by-10 / FM discriminator chain
+    others = None
+    if not args.no_other_configs:
+        others = other_configs(dev)
+
     # streaming serving loop: Poisson job arrivals at 2000/s, 1-64 channels,
     # blocks of 4096-1M samples, host buffers in and out, FP32 form
     serving = None
@@ -394,6 +477,7 @@ def run_ours(args) -> None:
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_step * args.steps,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "serving": serving,
+            "other_configs": others,
             "plain_fp32": plain,
             "tc_speedup_vs_plain_fp32": round(ms_per_step / plain["ms_per_step"], 3) ** -1 if plain else None,
         }
