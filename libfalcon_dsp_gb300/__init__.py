@@ -212,14 +212,22 @@ class MultiRateChannelizerCuda(_Handle):
     def _apply_device(self, x, out, stream):
         torch = _torch()
         x = _dev_c64(x)
-        cnt = self.out_count(x.numel())
         if out is None:
+            cnt = self.out_count(x.numel())
             out = [torch.empty(max(c, 1), dtype=torch.complex64, device=x.device) for c in cnt]
-        optr = (C.c_void_p * self.num_channels)(*[o.data_ptr() for o in out])
-        cap = (C.c_uint64 * self.num_channels)(*[o.numel() for o in out])
-        n_out = (C.c_uint64 * self.num_channels)()
+        # the ctypes pointer / capacity arrays are rebuilt only when the
+        # caller's output buffers change (streaming loops reuse them)
+        ptrs = tuple(o.data_ptr() for o in out)
+        oc = getattr(self, "_out_cache", None)
+        if oc is None or oc[0] != ptrs:
+            n = self.num_channels
+            oc = (ptrs, (C.c_void_p * n)(*ptrs), (C.c_uint64 * n)(*[o.numel() for o in out]), (C.c_uint64 * n)())
+            self._out_cache = oc
+        _, optr, cap, n_out = oc
         s = _stream_handle() if stream is None else stream
-        _capi.call("fdsp_channelizer_apply", self._h, _tptr(x), x.numel(), optr, cap, n_out, C.c_void_p(s))
+        st = _capi.lib().fdsp_channelizer_apply(self._h, x.data_ptr(), x.numel(), optr, cap, n_out, s)
+        if st:
+            _capi.check("fdsp_channelizer_apply", st)
         return [o[: n_out[i]] for i, o in enumerate(out)]
 
 

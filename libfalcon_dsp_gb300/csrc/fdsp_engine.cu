@@ -181,8 +181,9 @@ __device__ __forceinline__ void process_row(const float2* __restrict__ xs, const
 template <int NBMAX, bool kTapsSmem>
 __global__ void __launch_bounds__(kThreads, 3) poly_fp32_kernel(const __grid_constant__ PolyLaunch<NBMAX> L, int g) {
   extern __shared__ __align__(16) float2 xs[];
-  // g < 0: one launch over every group (small blocks), group = blockIdx.y
-  const GroupDesc& G = L.groups[g >= 0 ? g : (int)blockIdx.y];
+  // g < 0: one launch over several groups (small blocks), group =
+  // fuse_map[blockIdx.y + (-g - 1)]
+  const GroupDesc& G = L.groups[g >= 0 ? g : (int)L.fuse_map[(int)blockIdx.y - g - 1]];
   const int tile = blockIdx.x;
   if (tile >= G.ntiles) return;  // uniform over the CTA, before any barrier
   const int D = G.D, Qt = G.Qt, P = G.P;
@@ -715,18 +716,15 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
       if (st != FDSP_OK) return st;
     }
   }
-  // small blocks: every FP32 group in one launch (grid = tiles x groups,
-  // shared memory of the largest group) when they stage taps the same way;
-  // the per-launch cost then stops dominating short blocks
+  // small blocks: the FP32 groups in at most two launches (one per way of
+  // staging taps; grid = tiles x groups, shared memory of the largest group
+  // of the launch); the per-launch cost then stops dominating short blocks
   {
     bool fuse = ng > 1 && prof_ev_.empty();
     int64_t tiles = 0;
-    size_t fsmem = 0;
     for (int gi = 0; gi < ng && fuse; ++gi) {
-      const GroupDesc& gd = L.groups[gi];
-      fuse = !use_tc_for(group_of_d_[gd.D]) && gd.taps_smem == L.groups[0].taps_smem;
-      tiles += gd.ntiles;
-      fsmem = std::max(fsmem, (size_t)gd.smem_bytes);
+      fuse = !use_tc_for(group_of_d_[L.groups[gi].D]);
+      tiles += L.groups[gi].ntiles;
     }
     if (num_sms_ == 0) {
       int dev = 0;
@@ -735,13 +733,27 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
       if (num_sms_ <= 0) num_sms_ = 1;
     }
     if (fuse && tiles <= 3LL * num_sms_ && L.max_tiles > 0) {
-      auto kern = L.groups[0].taps_smem ? poly_fp32_kernel<NB, true> : poly_fp32_kernel<NB, false>;
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
-      if (e != cudaSuccess) return cuda_status(e);
-      kern<<<dim3((unsigned)L.max_tiles, (unsigned)ng), kThreads, fsmem, stream>>>(L, -1);
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return cuda_status(e);
-      launches_last_++;
+      int nm = 0;
+      for (int pass = 0; pass < 2; ++pass) {
+        const int first = nm;
+        size_t fsmem = 0;
+        int ftiles = 0;
+        for (int gi = 0; gi < ng; ++gi) {
+          const GroupDesc& gd = L.groups[gi];
+          if (gd.taps_smem != (pass == 0 ? 1 : 0) || gd.ntiles <= 0) continue;
+          L.fuse_map[nm++] = (int8_t)gi;
+          fsmem = std::max(fsmem, (size_t)gd.smem_bytes);
+          ftiles = std::max(ftiles, (int)gd.ntiles);
+        }
+        if (nm == first) continue;
+        auto kern = pass == 0 ? poly_fp32_kernel<NB, true> : poly_fp32_kernel<NB, false>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
+        if (e != cudaSuccess) return cuda_status(e);
+        kern<<<dim3((unsigned)ftiles, (unsigned)(nm - first)), kThreads, fsmem, stream>>>(L, -1 - first);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_status(e);
+        launches_last_++;
+      }
       ng = 0;  // nothing left for the per-group loop
     }
   }

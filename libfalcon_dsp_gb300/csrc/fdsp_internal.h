@@ -79,6 +79,7 @@ struct PolyLaunch {
   int32_t max_tiles;
   int32_t nws;
   const NcoConst* nco;      // [nch]
+  int8_t fuse_map[kMaxGroups];  // fused launches: group of blockIdx.y + offset
   GroupDesc groups[kMaxGroups];
   WorkSet<NB> ws[kMaxWorkSets];
   float2* out[kMaxChannels];         // output base of each channel for this launch
