@@ -50,7 +50,8 @@ enum fdsp_status {
     FDSP_ERR_CUDA = -4,            /* a CUDA runtime call failed; see fdsp_last_cuda_error() */
     FDSP_ERR_CAPACITY = -5,        /* an output buffer is smaller than the output count */
     FDSP_ERR_UNSUPPORTED = -6,     /* configuration outside this build's limits */
-    FDSP_ERR_NO_DEVICE = -7        /* no CUDA device is visible */
+    FDSP_ERR_NO_DEVICE = -7,       /* no CUDA device is visible */
+    FDSP_ERR_NOT_FOUND = -8        /* no predefined filter for the requested key */
 };
 
 /* Short text for a status code (static storage). */
@@ -71,6 +72,60 @@ int fdsp_freq_shift_params(uint32_t fs, int32_t f, uint32_t *rollover, double *o
 
 /* Replaces falcon_dsp::rat_approx (src/utilities/falcon_dsp_utils.cc:231-294). */
 int fdsp_rat_approx(double f, int64_t max_denom, int64_t *num, int64_t *den);
+
+/* ------------------------------------------------------------------------
+ * FM mono demodulator: falcon_dsp_fm_demodulator_cuda
+ * (hdr/signals/falcon_dsp_fm_demod_cuda.h:83-104,
+ * src/signals/falcon_dsp_fm_demod_cuda.cu) with every stage on the device:
+ * channelizer (NCO to signal_offset_hz, resample to 228 kS/s with the
+ * predefined REMEZ-64 filter) -> polar discriminator -> de-emphasis
+ * (one-pole IIR, 75 us or 50 us taps of src/signals/falcon_dsp_fm_demod.cc)
+ * -> mono decimator to 45.6 kS/s (REMEZ-64) -> x * (10000 / max |x| of the
+ * call) truncated to int16.
+ *   - create: deemphasis_tau must be 75e-6f or 50e-6f (else
+ *     FDSP_ERR_INVALID_ARG) and the table must hold input_sample_rate ->
+ *     228000 (else FDSP_ERR_NOT_FOUND), as the reference's initialize().
+ *   - apply: int16 audio for the call; the discriminator's first call emits
+ *     one sample less, and every stage's state carries to the next call.
+ * ---------------------------------------------------------------------- */
+#define FDSP_FM_RADIO_SAMPLE_RATE 228000u
+#define FDSP_FM_AUDIO_SAMPLE_RATE 45600u
+typedef struct fdsp_fm_demod fdsp_fm_demod;
+
+int fdsp_fm_demod_create(uint32_t input_sample_rate, int32_t signal_offset_hz, float deemphasis_tau,
+                         fdsp_fm_demod **out);
+int fdsp_fm_demod_destroy(fdsp_fm_demod *h);
+int fdsp_fm_demod_reset(fdsp_fm_demod *h);
+int fdsp_fm_demod_out_count(const fdsp_fm_demod *h, uint64_t n_in, uint64_t *n_out);
+int fdsp_fm_demod_apply(fdsp_fm_demod *h, const fdsp_cf32 *d_in, uint64_t n_in, int16_t *d_out, uint64_t out_cap,
+                        uint64_t *n_out, fdsp_stream_t stream);
+int fdsp_fm_demod_apply_host(fdsp_fm_demod *h, const fdsp_cf32 *h_in, uint64_t n_in, int16_t *h_out,
+                             uint64_t out_cap, uint64_t *n_out, fdsp_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Resampling filter design (host only: no device, no stream).
+ *
+ * fdsp_get_resample_fir_params replaces falcon_dsp::get_resample_fir_params
+ * (src/transform/falcon_dsp_fir_filter.cc:111-130): the predefined
+ * anti-alias lowpass for (input rate, output rate, taps, source), with its
+ * up/down rates.  taps: 16, 32, 64, 128, 256 or -1 (FILTER_TAPS_OPTIMAL);
+ * source: 0 REMEZ, 1 FIRLS (hdr/transform/falcon_dsp_predefined_fir_filter.h:
+ * 63-78).  The table is built with the library, by the reference's published
+ * recipe; a missing key returns FDSP_ERR_NOT_FOUND (the reference returns
+ * false).  *n_coeffs is always set; coeffs NULL or cap < *n_coeffs returns
+ * FDSP_ERR_CAPACITY, so a first call with coeffs NULL sizes the buffer.
+ *
+ * fdsp_design_resample_firls designs the same FIRLS lowpass for ANY rate
+ * pair: up/down from out/in, num_taps made odd, least-squares lowpass with
+ * edge 1/max(up, down) of Nyquist (closed form), scaled by up, Kaiser window
+ * (beta; the table uses 5).  Coefficients at full float precision (the table
+ * rounds them to 8 decimals).
+ * ---------------------------------------------------------------------- */
+int fdsp_get_resample_fir_params(uint32_t in_sps, uint32_t out_sps, int32_t taps, uint32_t source, uint32_t *up_rate,
+                                 uint32_t *down_rate, fdsp_cf32 *coeffs, uint32_t cap, uint32_t *n_coeffs);
+int fdsp_design_resample_firls(uint32_t in_sps, uint32_t out_sps, uint32_t num_taps, double kaiser_beta,
+                               uint32_t *up_rate, uint32_t *down_rate, fdsp_cf32 *coeffs, uint32_t cap,
+                               uint32_t *n_coeffs);
 
 /* Index bookkeeping of one resampler apply, in closed form: for n_in inputs
  * from state (phase, x_offset), the number of outputs the reference loop

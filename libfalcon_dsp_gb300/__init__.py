@@ -34,7 +34,13 @@ __all__ = [
     "FdspError", "FreqShiftCuda", "PolyphaseResamplerCuda", "MultiRateChannelizerCuda", "FirFilterCuda",
     "PolarDiscriminatorCuda", "freq_shift_params", "rat_approx", "freq_shift_cuda", "resample_cuda",
     "upfirdn_cuda", "fir_filter_cuda", "polar_discriminator_cuda", "channel", "resample_static",
+    "get_resample_fir_params", "design_resample_firls", "FILTER_TAPS_OPTIMAL", "REMEZ", "FIRLS",
+    "FmDemodulatorCuda",
 ]
+
+# filter_taps_e / filter_source_type_e (hdr/transform/falcon_dsp_predefined_fir_filter.h:63-78)
+FILTER_TAPS_OPTIMAL = -1
+REMEZ, FIRLS = 0, 1
 
 
 def _is_tensor(x) -> bool:
@@ -85,6 +91,34 @@ def rat_approx(f: float, max_denom: int) -> tuple[int, int]:
     n, d = C.c_int64(), C.c_int64()
     _capi.call("fdsp_rat_approx", float(f), int(max_denom), C.byref(n), C.byref(d))
     return n.value, d.value
+
+
+def _filter_call(fn: str, *args):
+    up, down, n = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    st = getattr(_capi.lib(), fn)(*args, C.byref(up), C.byref(down), None, 0, C.byref(n))
+    if st == _capi.FDSP_ERR_NOT_FOUND:
+        return None
+    if st not in (_capi.FDSP_OK, _capi.FDSP_ERR_CAPACITY):
+        _capi.check(fn, st)
+    h = np.empty(n.value, np.complex64)
+    _capi.call(fn, *args, C.byref(up), C.byref(down), h.ctypes.data, h.size, C.byref(n))
+    return up.value, down.value, h
+
+
+def get_resample_fir_params(input_sample_rate: int, output_sample_rate: int, taps: int = 64, source: int = REMEZ):
+    """get_resample_fir_params (src/transform/falcon_dsp_fir_filter.cc:111-130):
+    (up_rate, down_rate, complex64 coeffs) of the predefined anti-alias
+    filter, or None where the reference returns false (no such entry).
+    taps: 16/32/64/128/256 or FILTER_TAPS_OPTIMAL; source: REMEZ or FIRLS."""
+    return _filter_call("fdsp_get_resample_fir_params", int(input_sample_rate), int(output_sample_rate), int(taps),
+                        int(source))
+
+
+def design_resample_firls(input_sample_rate: int, output_sample_rate: int, num_taps: int, beta: float = 5.0):
+    """The FIRLS recipe of the predefined table for any rate pair (native
+    designer): (up_rate, down_rate, complex64 coeffs)."""
+    return _filter_call("fdsp_design_resample_firls", int(input_sample_rate), int(output_sample_rate),
+                        int(num_taps), float(beta))
 
 
 def channel(output_sample_rate_in_sps: int, freq_shift_in_hz: int, up_rate: int, down_rate: int,
@@ -228,7 +262,13 @@ class MultiRateChannelizerCuda(_Handle):
         st = _capi.lib().fdsp_channelizer_apply(self._h, x.data_ptr(), x.numel(), optr, cap, n_out, s)
         if st:
             _capi.check("fdsp_channelizer_apply", st)
-        return [o[: n_out[i]] for i, o in enumerate(out)]
+        # views of the output buffers, reused while the counts repeat
+        counts = tuple(n_out)
+        vc = getattr(self, "_view_cache", None)
+        if vc is None or vc[0] != ptrs or vc[1] != counts:
+            vc = (ptrs, counts, [o[:k] for o, k in zip(out, counts)])
+            self._view_cache = vc
+        return list(vc[2])
 
 
 class PolyphaseResamplerCuda(_Handle):
@@ -408,6 +448,68 @@ class PolarDiscriminatorCuda(_Handle):
         y = np.empty(max(xa.size, 1), np.float32)
         got = C.c_uint64()
         _capi.call("fdsp_polar_apply_host", self._h, _ptr(xa), xa.size, _ptr(y), C.byref(got),
+                   C.c_void_p(stream or 0))
+        return y[: got.value]
+
+
+class FmDemodulatorCuda(_Handle):
+    """falcon_dsp_fm_demodulator_cuda (hdr/signals/falcon_dsp_fm_demod_cuda.h:
+    83-104) with every stage on the GPU: channelizer to 228 kS/s (predefined
+    REMEZ-64 filter), polar discriminator, de-emphasis, mono decimator to
+    45.6 kS/s, rescale to int16 (x * 10000 / max |x| of the call)."""
+    _destroy = "fdsp_fm_demod_destroy"
+    AMERICAS_FM_DEEMPHASIS_TIME_CONSTANT = 75e-6
+    EUROPE_ASIA_FM_DEEMPHASIS_TIME_CONSTANT = 50e-6
+    FM_RADIO_SAMPLE_RATE_IN_SPS = 228000
+    FM_RADIO_AUDIO_SAMPLE_RATE_IN_SPS = 45600
+
+    def __init__(self, input_sample_rate: int | None = None, signal_offset_from_dc_in_hz: int = 0,
+                 deemphasis_time_constant: float = 75e-6):
+        super().__init__()
+        self.initialized = False
+        if input_sample_rate is not None:
+            if not self.initialize(input_sample_rate, signal_offset_from_dc_in_hz, deemphasis_time_constant):
+                raise FdspError("fdsp_fm_demod_create", _capi.FDSP_ERR_NOT_FOUND)
+
+    def initialize(self, input_sample_rate: int, signal_offset_from_dc_in_hz: int,
+                   deemphasis_time_constant: float = 75e-6) -> bool:
+        """False where the reference's initialize() fails: a second call, an
+        unsupported time constant, or no predefined filter for the rate."""
+        if self.initialized:
+            return False
+        st = _capi.lib().fdsp_fm_demod_create(int(input_sample_rate), int(np.int32(signal_offset_from_dc_in_hz)),
+                                              float(np.float32(deemphasis_time_constant)), C.byref(self._h))
+        if st in (_capi.FDSP_ERR_NOT_FOUND, -1):
+            return False
+        _capi.check("fdsp_fm_demod_create", st)
+        self.initialized = True
+        return True
+
+    def reset_state(self) -> None:
+        _capi.call("fdsp_fm_demod_reset", self._h)
+
+    def out_count(self, n_in: int) -> int:
+        v = C.c_uint64()
+        _capi.call("fdsp_fm_demod_out_count", self._h, int(n_in), C.byref(v))
+        return v.value
+
+    def demod_mono(self, x, out=None, stream: int | None = None):
+        """int16 mono audio of one block (numpy in -> numpy out, or CUDA
+        complex64 tensor in -> CUDA int16 tensor out)."""
+        n = self.out_count(x.numel() if _is_tensor(x) else np.asarray(x).shape[0])
+        got = C.c_uint64()
+        if _is_tensor(x):
+            torch = _torch()
+            x = _dev_c64(x)
+            if out is None:
+                out = torch.empty(max(n, 1), dtype=torch.int16, device=x.device)
+            s = _stream_handle() if stream is None else stream
+            _capi.call("fdsp_fm_demod_apply", self._h, _tptr(x), x.numel(), _tptr(out), out.numel(), C.byref(got),
+                       C.c_void_p(s))
+            return out[: got.value]
+        xa = _c64(x)
+        y = np.empty(max(n, 1), np.int16)
+        _capi.call("fdsp_fm_demod_apply_host", self._h, _ptr(xa), xa.size, _ptr(y), y.size, C.byref(got),
                    C.c_void_p(stream or 0))
         return y[: got.value]
 

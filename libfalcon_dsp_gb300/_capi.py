@@ -22,7 +22,9 @@ STATUS = {
     -5: "FDSP_ERR_CAPACITY",
     -6: "FDSP_ERR_UNSUPPORTED",
     -7: "FDSP_ERR_NO_DEVICE",
+    -8: "FDSP_ERR_NOT_FOUND",
 }
+FDSP_ERR_NOT_FOUND = -8
 
 
 class cf32(C.Structure):
@@ -62,6 +64,8 @@ SIGNATURES = {
     "fdsp_version": [],
     "fdsp_freq_shift_params": [_u32, _i32, _pu32, _pdbl],
     "fdsp_rat_approx": [_dbl, _i64, _pi64, _pi64],
+    "fdsp_get_resample_fir_params": [_u32, _u32, _i32, _u32, _pu32, _pu32, _vp, _u32, _pu32],
+    "fdsp_design_resample_firls": [_u32, _u32, _u32, _dbl, _pu32, _pu32, _vp, _u32, _pu32],
     "fdsp_polyphase_advance": [_u32, _u32, _u32, _u64, _u64, _pu64, _pu32, _pu64],
     "fdsp_channelizer_create": [_u32, C.POINTER(channel_cfg), _u32, _pp],
     "fdsp_channelizer_destroy": [_vp],
@@ -109,6 +113,12 @@ SIGNATURES = {
     "fdsp_fir_reset": [_vp],
     "fdsp_fir_apply": [_vp, _vp, _u64, _vp, _vp],
     "fdsp_fir_apply_host": [_vp, _vp, _u64, _vp, _vp],
+    "fdsp_fm_demod_create": [_u32, _i32, C.c_float, _pp],
+    "fdsp_fm_demod_destroy": [_vp],
+    "fdsp_fm_demod_reset": [_vp],
+    "fdsp_fm_demod_out_count": [_vp, _u64, _pu64],
+    "fdsp_fm_demod_apply": [_vp, _vp, _u64, _vp, _u64, _pu64, _vp],
+    "fdsp_fm_demod_apply_host": [_vp, _vp, _u64, _vp, _u64, _pu64, _vp],
     "fdsp_polar_create": [_pp],
     "fdsp_polar_destroy": [_vp],
     "fdsp_polar_reset": [_vp],

@@ -23,10 +23,11 @@ OBJ = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libfalcon_dsp_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
+GEN = os.path.join(OBJ, "gen")  # generated sources (the predefined filter table)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-                     "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(CPP, "include")]
+                     "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(CPP, "include"), "-I", GEN]
 
 
 def nvcc() -> str:
@@ -49,9 +50,9 @@ def sources() -> list[str]:
 
 def _headers() -> list[str]:
     hs = []
-    for d in (CSRC, INCLUDE, os.path.join(CPP, "include")):
+    for d in (CSRC, INCLUDE, os.path.join(CPP, "include"), GEN):
         for r, _, fs in os.walk(d):
-            hs += [os.path.join(r, f) for f in fs if f.endswith((".h", ".cuh", ".hpp"))]
+            hs += [os.path.join(r, f) for f in fs if f.endswith((".h", ".cuh", ".hpp", ".inc"))]
     return hs
 
 
@@ -68,9 +69,21 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
+def _gen_filter_table() -> None:
+    """The predefined resampling filters (filter_design.py, scipy at build
+    time) as a C++ include, regenerated when the generator changes."""
+    out = os.path.join(GEN, "fdsp_filter_table.inc")
+    gen = os.path.join(PKG, "filter_design.py")
+    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(gen):
+        return
+    from . import filter_design
+    filter_design.write_table_inc(out)
+
+
 def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
+    _gen_filter_table()
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra or []), srcs))

@@ -24,25 +24,6 @@ int cuda_status(cudaError_t e) {
   return FDSP_ERR_CUDA;
 }
 
-// Grow-only device buffer used by the *_apply_host entry points.
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-  int ensure(size_t want) {
-    if (want <= bytes) return FDSP_OK;
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e != cudaSuccess) return cuda_status(e);
-    bytes = want;
-    return FDSP_OK;
-  }
-};
-
 }  // namespace fdsp
 
 using namespace fdsp;
@@ -85,12 +66,6 @@ struct fdsp_polar {
   }
 };
 
-#define FDSP_TRY(expr)              \
-  do {                              \
-    int st_ = (expr);               \
-    if (st_ != FDSP_OK) return st_; \
-  } while (0)
-
 extern "C" {
 
 const char* fdsp_status_string(int status) {
@@ -103,6 +78,7 @@ const char* fdsp_status_string(int status) {
     case FDSP_ERR_CAPACITY: return "output buffer too small";
     case FDSP_ERR_UNSUPPORTED: return "configuration outside this build's limits";
     case FDSP_ERR_NO_DEVICE: return "no CUDA device";
+    case FDSP_ERR_NOT_FOUND: return "no predefined filter for this key";
     default: return "unknown status";
   }
 }

@@ -5,10 +5,17 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <map>
 #include <vector>
 
 #include "fdsp_c.h"
+
+#define FDSP_TRY(expr)              \
+  do {                              \
+    int st_ = (expr);               \
+    if (st_ != FDSP_OK) return st_; \
+  } while (0)
 
 namespace fdsp {
 
@@ -181,6 +188,33 @@ struct TcChunk {
 
 // CUDA error -> status, remembering the CUDA code for fdsp_last_cuda_error().
 int cuda_status(cudaError_t e);
+
+// Grow-only device buffer (scratch of the *_apply_host entry points and of
+// multi-stage pipelines).
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) {
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  int ensure(size_t want) {
+    if (want <= bytes) return FDSP_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) return cuda_status(e);
+    bytes = want;
+    return FDSP_OK;
+  }
+};
 void set_last_cuda_error(int code);
 
 // ---------------------------------------------------------------------------

@@ -177,6 +177,31 @@ def fm_chain(n: int = 1 << 26, seed: int = 2027, device=None):
     return x, int(FM_FS), h.astype(np.complex64), tones
 
 
+FM_RADIO_FS = 1140000  # the input rate of the FM receiver's predefined filters
+
+
+def fm_station(n: int, station_hz: int = -150000, seed: int = 2031, fs: int = FM_RADIO_FS, snr_db: float = 25.0):
+    """A broadcast FM station at `station_hz` in a complex baseband capture at
+    `fs` (a receiver tuned to it shifts by -station_hz): message of 3 tones in
+    300 Hz - 12 kHz, 75 kHz peak deviation, plus a weaker station 550 kHz
+    away and AWGN.  Returns (x complex64, tone_freqs)."""
+    rng = np.random.default_rng(seed)
+    tones = np.sort(rng.uniform(300.0, 12000.0, 3))
+    amps = rng.uniform(0.3, 1.0, 3)
+    amps /= amps.sum()
+    ph = rng.uniform(0, 2 * np.pi, 3)
+    t = np.arange(n, dtype=np.float64) / fs
+    integ = np.zeros(n)
+    for f, a, p in zip(tones, amps, ph):
+        integ += a * (np.sin(2 * np.pi * f * t + p) - np.sin(p)) / (2 * np.pi * f)
+    x = np.exp(1j * (2 * np.pi * 75e3 * integ + 2 * np.pi * station_hz * t))
+    other = station_hz + 550000
+    x += 0.3 * np.exp(1j * (2 * np.pi * 20e3 * np.sin(2 * np.pi * 700.0 * t) / 700.0 + 2 * np.pi * other * t))
+    sigma = np.sqrt(10 ** (-snr_db / 10) / 2)
+    x = x + sigma * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    return x.astype(np.complex64), tones
+
+
 def audio_snr_db(audio: np.ndarray, fs_audio: float, tones, skip: int = 1024) -> float:
     """Recovered-audio SNR: least-squares fit of the known message tones (and
     a constant) to the demodulated audio, fit power over residual power."""

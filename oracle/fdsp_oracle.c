@@ -17,6 +17,7 @@
  *   - needed_out_count           src/transform/falcon_dsp_polyphase_resampler.cc:216-228
  *   - FIR apply / state          src/transform/falcon_dsp_fir_filter.cc:177-284
  *   - polar discriminator        src/transform/falcon_dsp_polar_discriminator.cc:134-171
+ *   - IIR filter                 src/transform/falcon_dsp_iir_filter.cc:67-110, 235-396
  *   - rat_approx                 src/utilities/falcon_dsp_utils.cc:231-294
  *
  * Two arithmetic flavours exist for the NCO and the resampler:
@@ -411,6 +412,123 @@ uint64_t orc_polar_apply_f32(orc_polar *p, const float *in, uint64_t count, floa
     p->prev_re = in[2 * (count - 1)];
     p->prev_im = in[2 * (count - 1) + 1];
     return n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* IIR filter (direct form, complex<float> taps)                              */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    uint32_t nb, na;
+    float *b, *a;    /* interleaved complex, a[0] = 1 after normalisation */
+    float *xs;       /* last nb inputs, oldest first (m_input_state) */
+    uint32_t nxs;
+    float *ys;       /* last na - 1 outputs, oldest first (m_prev_outputs) */
+    uint32_t nys;
+} orc_iir;
+
+/* complex<float> product and quotient, one rounding per operation */
+static void cmulf(float ar, float ai, float br, float bi, float *cr, float *ci)
+{
+    float t1 = ar * br, t2 = ai * bi, t3 = ar * bi, t4 = ai * br;
+    *cr = t1 - t2;
+    *ci = t3 + t4;
+}
+static void cdivf(float ar, float ai, float br, float bi, float *cr, float *ci)
+{
+    float d = br * br + bi * bi;
+    *cr = (ar * br + ai * bi) / d;
+    *ci = (ai * br - ar * bi) / d;
+}
+
+/* iir_filter.cc:67-110: b and a divided by a[0] unless a[0].real() == 1. */
+orc_iir *orc_iir_new(const float *b, uint32_t nb, const float *a, uint32_t na)
+{
+    orc_iir *f = (orc_iir *)calloc(1, sizeof(orc_iir));
+    if (!f || nb == 0 || na == 0) { free(f); return NULL; }
+    f->nb = nb;
+    f->na = na;
+    f->b = (float *)malloc(2 * (size_t)nb * sizeof(float));
+    f->a = (float *)malloc(2 * (size_t)na * sizeof(float));
+    f->xs = (float *)calloc(2 * (size_t)nb, sizeof(float));
+    f->ys = (float *)calloc(2 * (size_t)na, sizeof(float));
+    memcpy(f->b, b, 2 * (size_t)nb * sizeof(float));
+    memcpy(f->a, a, 2 * (size_t)na * sizeof(float));
+    if (a[0] != 1.0f) {
+        for (uint32_t i = 0; i < nb; ++i) cdivf(b[2 * i], b[2 * i + 1], a[0], a[1], &f->b[2 * i], &f->b[2 * i + 1]);
+        for (uint32_t i = 1; i < na; ++i) cdivf(a[2 * i], a[2 * i + 1], a[0], a[1], &f->a[2 * i], &f->a[2 * i + 1]);
+    }
+    return f;
+}
+
+void orc_iir_free(orc_iir *f)
+{
+    if (!f) return;
+    free(f->b); free(f->a); free(f->xs); free(f->ys); free(f);
+}
+
+void orc_iir_reset(orc_iir *f) { f->nxs = 0; f->nys = 0; }
+
+/* iir_filter.cc:235-396: acc = sum_k b[k] x[n-k] (inputs of this call
+ * newest first, then the saved inputs), minus sum_k a[k] y[n-k] over the
+ * saved outputs, newest first; one output per input.  Returns count (0 for
+ * an empty input, where the reference returns false). */
+uint64_t orc_iir_apply_f32(orc_iir *f, const float *in, uint64_t count, float *out)
+{
+    if (count == 0) return 0;
+    for (uint64_t n = 0; n < count; ++n) {
+        float accr = 0.f, acci = 0.f, pr, pi;
+        uint32_t k = 0;
+        if (n < f->nb) {
+            for (int64_t i = (int64_t)n; i >= 0; --i, ++k) {
+                cmulf(in[2 * i], in[2 * i + 1], f->b[2 * k], f->b[2 * k + 1], &pr, &pi);
+                accr = accr + pr; acci = acci + pi;
+            }
+            for (int64_t s = (int64_t)f->nxs - 1; s >= 0 && k < f->nb; --s, ++k) {
+                cmulf(f->xs[2 * s], f->xs[2 * s + 1], f->b[2 * k], f->b[2 * k + 1], &pr, &pi);
+                accr = accr + pr; acci = acci + pi;
+            }
+        } else {
+            for (k = 0; k < f->nb; ++k) {
+                const uint64_t i = n - k;
+                cmulf(in[2 * i], in[2 * i + 1], f->b[2 * k], f->b[2 * k + 1], &pr, &pi);
+                accr = accr + pr; acci = acci + pi;
+            }
+        }
+        uint32_t j = 1;
+        for (int64_t s = (int64_t)f->nys - 1; s >= 0 && j < f->na; --s, ++j) {
+            cmulf(f->ys[2 * s], f->ys[2 * s + 1], f->a[2 * j], f->a[2 * j + 1], &pr, &pi);
+            accr = accr - pr; acci = acci - pi;
+        }
+        out[2 * n] = accr;
+        out[2 * n + 1] = acci;
+        /* keep the last na - 1 outputs */
+        if (f->na > 1) {
+            if (f->nys == f->na - 1) {
+                memmove(f->ys, f->ys + 2, 2 * (size_t)(f->nys - 1) * sizeof(float));
+                f->nys--;
+            }
+            f->ys[2 * f->nys] = accr;
+            f->ys[2 * f->nys + 1] = acci;
+            f->nys++;
+        }
+    }
+    /* input state: the last nb inputs (iir_filter.cc:380-396) */
+    if (count >= f->nb) {
+        memcpy(f->xs, in + 2 * (count - f->nb), 2 * (size_t)f->nb * sizeof(float));
+        f->nxs = f->nb;
+    } else {
+        for (uint64_t i = 0; i < count; ++i) {
+            if (f->nxs == f->nb) {
+                memmove(f->xs, f->xs + 2, 2 * (size_t)(f->nb - 1) * sizeof(float));
+                f->nxs--;
+            }
+            f->xs[2 * f->nxs] = in[2 * i];
+            f->xs[2 * f->nxs + 1] = in[2 * i + 1];
+            f->nxs++;
+        }
+    }
+    return count;
 }
 
 /* ------------------------------------------------------------------------ */

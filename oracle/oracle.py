@@ -100,6 +100,10 @@ def port_lib():
             "orc_polar_reset": (None, [_vp]),
             "orc_polar_apply_f32": (_u64, [_vp, _fp, _u64, _fp]),
             "orc_rat_approx": (None, [_dbl, _i64, C.POINTER(_i64), C.POINTER(_i64)]),
+            "orc_iir_new": (_vp, [_fp, _u32, _fp, _u32]),
+            "orc_iir_free": (None, [_vp]),
+            "orc_iir_reset": (None, [_vp]),
+            "orc_iir_apply_f32": (_u64, [_vp, _fp, _u64, _fp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -288,6 +292,69 @@ class Polar:
         return y[:n]
 
 
+class IIR:
+    """falcon_dsp_iir_filter (src/transform/falcon_dsp_iir_filter.cc) restated:
+    complex<float> direct form, b/a normalised by a[0]."""
+
+    def __init__(self, b, a):
+        self._lib = port_lib()
+        b, a = as_c64(b), as_c64(a)
+        self._h = self._lib.orc_iir_new(_f32p(b.view(np.float32)), b.size, _f32p(a.view(np.float32)), a.size)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.orc_iir_free(self._h)
+            self._h = None
+
+    def reset_state(self):
+        self._lib.orc_iir_reset(self._h)
+
+    def apply(self, x) -> np.ndarray:
+        x = as_c64(x)
+        y = np.empty(max(x.size, 1), dtype=np.complex64)
+        n = self._lib.orc_iir_apply_f32(self._h, _f32p(x.view(np.float32)), x.size, _f32p(y.view(np.float32)))
+        return y[:n]
+
+
+# de-emphasis taps (b0, a1) of src/signals/falcon_dsp_fm_demod.cc:119-133
+DEEMPHASIS = {75e-6: (0.064493014968382223, -0.93550698503161778),
+              50e-6: (0.095162581964040482, -0.90483741803595952)}
+
+
+class FmDemod:
+    """falcon_dsp_fm_demodulator::demod_mono (src/signals/falcon_dsp_fm_demod.cc)
+    restated from the oracle's own stages: NCO + isolation resampler, polar
+    discriminator, de-emphasis IIR, mono resampler, then x * (10000 / max |x|)
+    truncated to int16.  The two resampling filters are given (the predefined
+    REMEZ-64 entries of the reference's table)."""
+
+    def __init__(self, fs: int, offset_hz: int, iso, mono, tau: float = 75e-6):
+        up, down, h = iso
+        mup, mdown, mh = mono
+        self.chan = Channelizer(fs, [dict(freq_shift_in_hz=int(offset_hz), up_rate=up, down_rate=down, coeffs=h)])
+        self.polar = Polar()
+        b0, a1 = DEEMPHASIS[tau]
+        self.iir = IIR(np.array([b0], np.complex64), np.array([1.0, a1], np.complex64))
+        self.mono = Resampler(mup, mdown, mh)
+
+    def reset_state(self):
+        self.chan.reset_state()
+        self.polar.reset_state()
+        self.iir.reset_state()
+        self.mono.reset_state()
+
+    def demod_mono(self, x) -> np.ndarray:
+        iso = self.chan.apply(x)[0]
+        pol = self.polar.apply(iso)
+        emph = self.iir.apply(pol.astype(np.complex64)).real.astype(np.float32) if pol.size else pol
+        m = self.mono.apply(emph.astype(np.complex64)).real.astype(np.float32) if emph.size else emph
+        if m.size == 0:
+            return np.zeros(0, np.int16)
+        amax = np.float32(np.max(np.abs(m)))
+        scale = np.float32(10000.0 / float(amax))
+        return np.trunc(m * scale).astype(np.int16)
+
+
 # --------------------------------------------------------------------------
 # The reference's own CPU classes (oracle/_ref), when built
 # --------------------------------------------------------------------------
@@ -329,6 +396,16 @@ def ref_lib():
             "ref_polar_reset": (None, [_vp]),
             "ref_polar_apply": (_u64, [_vp, _fp, _u64, _fp]),
             "ref_rat_approx": (None, [_dbl, _i64, C.POINTER(_i64), C.POINTER(_i64)]),
+            "ref_get_resample_fir_params": (_u32, [_u32, _u32, C.c_int32, _u32, C.POINTER(_u32), C.POINTER(_u32),
+                                                   _fp, _u32]),
+            "ref_iir_new": (_vp, [_fp, _u32, _fp, _u32]),
+            "ref_iir_free": (None, [_vp]),
+            "ref_iir_reset": (None, [_vp]),
+            "ref_iir_apply": (_u64, [_vp, _fp, _u64, _fp]),
+            "ref_fm_new": (_vp, [_u32, _i32, C.c_float]),
+            "ref_fm_free": (None, [_vp]),
+            "ref_fm_reset": (None, [_vp]),
+            "ref_fm_demod_mono": (_u64, [_vp, _fp, _u64, C.POINTER(C.c_int16), _u64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -336,6 +413,60 @@ def ref_lib():
             fn.argtypes = args
         _ref = lib
     return _ref
+
+
+def ref_get_resample_fir_params(in_sps: int, out_sps: int, taps: int, source: int):
+    """(up, down, float32 taps) from the reference's own table, or None."""
+    up, down = _u32(), _u32()
+    buf = np.zeros(4096, np.float32)
+    n = ref_lib().ref_get_resample_fir_params(in_sps, out_sps, taps, source, C.byref(up), C.byref(down),
+                                              _f32p(buf), buf.size)
+    if n == 0:
+        return None
+    return up.value, down.value, buf[:n].copy()
+
+
+class RefIIR:
+    def __init__(self, b, a):
+        b, a = as_c64(b), as_c64(a)
+        self._h = ref_lib().ref_iir_new(_f32p(b.view(np.float32)), b.size, _f32p(a.view(np.float32)), a.size)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            ref_lib().ref_iir_free(self._h)
+            self._h = None
+
+    def reset_state(self):
+        ref_lib().ref_iir_reset(self._h)
+
+    def apply(self, x):
+        x = as_c64(x)
+        y = np.empty(max(x.size, 1), np.complex64)
+        n = ref_lib().ref_iir_apply(self._h, _f32p(x.view(np.float32)), x.size, _f32p(y.view(np.float32)))
+        return y[:n]
+
+
+class RefFmDemod:
+    """The reference's own CPU falcon_dsp_fm_demodulator (None handle when
+    its initialize() fails)."""
+
+    def __init__(self, fs, offset_hz, tau=75e-6):
+        self._h = ref_lib().ref_fm_new(int(fs), int(offset_hz), float(tau))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            ref_lib().ref_fm_free(self._h)
+            self._h = None
+
+    def reset_state(self):
+        ref_lib().ref_fm_reset(self._h)
+
+    def demod_mono(self, x):
+        x = as_c64(x)
+        y = np.empty(x.size + 16, np.int16)
+        n = ref_lib().ref_fm_demod_mono(self._h, _f32p(x.view(np.float32)), x.size,
+                                        y.ctypes.data_as(C.POINTER(C.c_int16)), y.size)
+        return y[:n].copy()
 
 
 class RefResampler:

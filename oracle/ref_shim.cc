@@ -15,12 +15,15 @@
  *   falcon_dsp_polar_discriminator     hdr/transform/falcon_dsp_polar_discriminator.h:97-114
  *   rat_approx                         hdr/utilities/falcon_dsp_utils.h
  */
+#include <algorithm>
 #include <complex>
 #include <cstdint>
 #include <cstring>
 #include <vector>
 
+#include "signals/falcon_dsp_fm_demod.h"
 #include "transform/falcon_dsp_fir_filter.h"
+#include "transform/falcon_dsp_iir_filter.h"
 #include "transform/falcon_dsp_freq_shift.h"
 #include "transform/falcon_dsp_multi_rate_channelizer.h"
 #include "transform/falcon_dsp_polar_discriminator.h"
@@ -169,7 +172,58 @@ uint64_t ref_polar_apply(void *o, const float *in, uint64_t n, float *out)
     return vout.size();
 }
 
+/* ---- IIR filter and FM demodulator ----------------------------------------- */
+void *ref_iir_new(const float *b, uint32_t nb, const float *a, uint32_t na)
+{
+    auto vb = to_vec(b, nb), va = to_vec(a, na);
+    auto *o = new falcon_dsp::falcon_dsp_iir_filter();
+    if (!o->initialize(vb, va)) { delete o; return nullptr; }
+    return o;
+}
+void ref_iir_free(void *o) { delete static_cast<falcon_dsp::falcon_dsp_iir_filter *>(o); }
+void ref_iir_reset(void *o) { static_cast<falcon_dsp::falcon_dsp_iir_filter *>(o)->reset_state(); }
+uint64_t ref_iir_apply(void *o, const float *in, uint64_t n, float *out)
+{
+    auto vin = to_vec(in, n);
+    std::vector<cf> vout;
+    static_cast<falcon_dsp::falcon_dsp_iir_filter *>(o)->apply(vin, vout);
+    if (!vout.empty()) std::memcpy(out, vout.data(), vout.size() * sizeof(cf));
+    return vout.size();
+}
+
+void *ref_fm_new(uint32_t fs, int32_t offset, float tau)
+{
+    auto *o = new falcon_dsp::falcon_dsp_fm_demodulator();
+    if (!o->initialize(fs, offset, tau)) { delete o; return nullptr; }
+    return o;
+}
+void ref_fm_free(void *o) { delete static_cast<falcon_dsp::falcon_dsp_fm_demodulator *>(o); }
+void ref_fm_reset(void *o) { static_cast<falcon_dsp::falcon_dsp_fm_demodulator *>(o)->reset_state(); }
+/* demod_mono; returns the int16 count (the reference's bool is count > 0) */
+uint64_t ref_fm_demod_mono(void *o, const float *in, uint64_t n, int16_t *out, uint64_t cap)
+{
+    auto vin = to_vec(in, n);
+    std::vector<int16_t> vout;
+    static_cast<falcon_dsp::falcon_dsp_fm_demodulator *>(o)->demod_mono(vin, vout);
+    if (!vout.empty()) std::memcpy(out, vout.data(), std::min<uint64_t>(vout.size(), cap) * sizeof(int16_t));
+    return vout.size();
+}
+
 /* ---- utilities ---------------------------------------------------------- */
 void ref_rat_approx(double f, int64_t md, int64_t *num, int64_t *den) { falcon_dsp::rat_approx(f, md, *num, *den); }
+
+/* get_resample_fir_params over the reference's own predefined table: returns
+ * the coefficient count (0 when the reference returns false); real parts into
+ * `re` when cap allows. */
+uint32_t ref_get_resample_fir_params(uint32_t in_sps, uint32_t out_sps, int32_t taps, uint32_t source, uint32_t *up,
+                                     uint32_t *down, float *re, uint32_t cap)
+{
+    std::vector<cf> h;
+    if (!falcon_dsp::get_resample_fir_params(in_sps, out_sps, static_cast<filter_taps_e>(taps),
+                                             static_cast<filter_source_type_e>(source), *up, *down, h))
+        return 0;
+    for (size_t i = 0; i < h.size() && i < cap; ++i) re[i] = h[i].real();
+    return static_cast<uint32_t>(h.size());
+}
 
 } /* extern "C" */

@@ -10,11 +10,13 @@
 #include <string>
 #include <vector>
 
+#include "signals/falcon_dsp_fm_demod_cuda.h"
 #include "transform/falcon_dsp_fir_filter_cuda.h"
 #include "transform/falcon_dsp_freq_shift_cuda.h"
 #include "transform/falcon_dsp_multi_rate_channelizer_cuda.h"
 #include "transform/falcon_dsp_polar_discriminator_cuda.h"
 #include "transform/falcon_dsp_polyphase_resampler_cuda.h"
+#include "transform/falcon_dsp_predefined_fir_filter.h"
 #include "transform/falcon_dsp_resample_cuda.h"
 
 using cvec = std::vector<std::complex<float>>;
@@ -164,6 +166,38 @@ int main(int argc, char** argv) {
         dump("rsc_taps.bin", taps);
         dump("rsc_in.bin", in);
         dump("rsc_out.bin", out);
+    }
+    // predefined filter lookup (host only)
+    {
+        uint32_t up = 0, down = 0;
+        cvec h;
+        check(get_resample_fir_params(228000, 45600, filter_taps_e::FILTER_TAPS_64, filter_source_type_e::REMEZ, up,
+                                      down, h),
+              "get_resample_fir_params");
+        check(up == 1 && down == 5 && h.size() == 64, "predefined 228k -> 45.6k");
+        dump("pf_taps.bin", h);
+        check(!get_resample_fir_params(48000, 44100, filter_taps_e::FILTER_TAPS_64, filter_source_type_e::REMEZ, up,
+                                       down, h) && h.empty(),
+              "missing key");
+    }
+    // FM demodulator: station at -150 kHz in a 1.14 MS/s capture
+    {
+        falcon_dsp_fm_demodulator_cuda fm;
+        check(!fm.initialize(1140000, 150000, 60e-6f), "fm bad time constant");
+        check(fm.initialize(1140000, 150000), "fm initialize");
+        check(!fm.initialize(1140000, 150000), "fm initialize once");
+        for (int b = 0; b < 2; ++b) {
+            cvec in(114000 + 7 * b);
+            for (size_t i = 0; i < in.size(); ++i) {
+                const double t = (double)(i + b * 114000) / 1140000.0;
+                const double ph = -2 * M_PI * 150000.0 * t + 5.0 * std::sin(2 * M_PI * 1000.0 * t);
+                in[i] = {(float)std::cos(ph), (float)std::sin(ph)};
+            }
+            std::vector<int16_t> out;
+            check(fm.demod_mono(in, out), "fm demod_mono");
+            dump("fm_in" + std::to_string(b) + ".bin", in);
+            dump("fm_out" + std::to_string(b) + ".bin", out);
+        }
     }
     std::printf(g_fail ? "dropin_check: FAILED\n" : "dropin_check: ok\n");
     return g_fail;

@@ -19,6 +19,7 @@ import subprocess
 import numpy as np
 import pytest
 
+from libfalcon_dsp_gb300 import filter_design as FD
 from oracle import oracle as O
 from tests.golden_io import rel_rms
 
@@ -121,3 +122,16 @@ def test_dropin_classes_match_oracle(tmp_path):
     ref = O.Resampler(147, 160, _c64(d, "rsc_taps.bin")).apply(_c64(d, "rsc_in.bin"))
     got = _c64(d, "rsc_out.bin")
     assert got.size == ref.size and rel_rms(got, ref) <= 1e-5
+
+    # predefined filter lookup: the generator's REMEZ-64 228 kS/s -> 45.6 kS/s entry
+    table = FD.design_table()
+    want = table[(228000, 45600, 64, FD.REMEZ)]
+    assert np.array_equal(_c64(d, "pf_taps.bin").real, want[2])
+
+    # FM demodulator, two streaming calls, against the oracle's demod_mono
+    om = O.FmDemod(1140000, 150000, table[(1140000, 228000, 64, FD.REMEZ)], want)
+    for b in range(2):
+        ref = om.demod_mono(_c64(d, f"fm_in{b}.bin"))
+        got = np.fromfile(os.path.join(d, f"fm_out{b}.bin"), dtype=np.int16)
+        assert got.size == ref.size and got.size > 0
+        assert np.max(np.abs(got.astype(np.int32) - ref.astype(np.int32))) <= 1
