@@ -212,6 +212,17 @@ int fdsp_channelizer_group_info(const fdsp_channelizer *h, uint32_t group, uint3
 /* apply(in, out) on host buffers (copies in, computes, copies out, syncs). */
 int fdsp_channelizer_apply_host(fdsp_channelizer *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,
                                 const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);
+/* int16 front end: n_in complex int16 samples (interleaved I, Q: the layout
+ * of std::complex<int16_t> and of the reference's "<2h" sample files,
+ * src/utilities/falcon_dsp_utils.cc:534-742), converted to float inside the
+ * first kernel that reads them, so the block crosses HBM (and PCIe) at 4
+ * bytes a sample.  Outputs as fdsp_channelizer_apply; equal to converting
+ * first, as the reference's int16 overloads do (freq_shift.cc:133-162). */
+int fdsp_channelizer_apply_ci16(fdsp_channelizer *h, const int16_t *d_in, uint64_t n_in, fdsp_cf32 *const *d_out,
+                                const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);
+int fdsp_channelizer_apply_ci16_host(fdsp_channelizer *h, const int16_t *h_in, uint64_t n_in,
+                                     fdsp_cf32 *const *h_out, const uint64_t *out_cap, uint64_t *n_out,
+                                     fdsp_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Polyphase resampler (single channel, no shift).
@@ -238,6 +249,9 @@ int fdsp_resampler_state(const fdsp_resampler *h, uint32_t *coeff_phase, uint64_
 int fdsp_resampler_apply(fdsp_resampler *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *d_out, uint64_t out_cap,
                          uint64_t *n_out, fdsp_stream_t stream);
 int fdsp_resampler_apply_host(fdsp_resampler *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *h_out,
+                              uint64_t out_cap, uint64_t *n_out, fdsp_stream_t stream);
+/* complex int16 input (see fdsp_channelizer_apply_ci16), complex64 output */
+int fdsp_resampler_apply_ci16(fdsp_resampler *h, const int16_t *d_in, uint64_t n_in, fdsp_cf32 *d_out,
                               uint64_t out_cap, uint64_t *n_out, fdsp_stream_t stream);
 
 /* ------------------------------------------------------------------------
@@ -291,6 +305,12 @@ int fdsp_freq_shift_apply(fdsp_freq_shift *h, const fdsp_cf32 *d_in, uint64_t n_
                           fdsp_stream_t stream);
 int fdsp_freq_shift_apply_host(fdsp_freq_shift *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,
                                fdsp_stream_t stream);
+/* int16 overload (src/transform/falcon_dsp_freq_shift.cc:133-162): complex
+ * int16 in, converted on load; complex int16 out, truncated toward zero. */
+int fdsp_freq_shift_apply_ci16(fdsp_freq_shift *h, const int16_t *d_in, uint64_t n_in, int16_t *const *d_out,
+                               fdsp_stream_t stream);
+int fdsp_freq_shift_apply_ci16_host(fdsp_freq_shift *h, const int16_t *h_in, uint64_t n_in, int16_t *const *h_out,
+                                    fdsp_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * FIR filter with complex taps, output length = input length.
@@ -305,6 +325,11 @@ int fdsp_fir_destroy(fdsp_fir *h);
 int fdsp_fir_reset(fdsp_fir *h);
 int fdsp_fir_apply(fdsp_fir *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *d_out, fdsp_stream_t stream);
 int fdsp_fir_apply_host(fdsp_fir *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *h_out, fdsp_stream_t stream);
+/* int16 overload (src/transform/falcon_dsp_fir_filter.cc:151-175): complex
+ * int16 in (converted inside the filter kernel), complex int16 out
+ * (truncated toward zero). */
+int fdsp_fir_apply_ci16(fdsp_fir *h, const int16_t *d_in, uint64_t n_in, int16_t *d_out, fdsp_stream_t stream);
+int fdsp_fir_apply_ci16_host(fdsp_fir *h, const int16_t *h_in, uint64_t n_in, int16_t *h_out, fdsp_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Polar discriminator (FM demodulation core): out[n] = arg(x[n] conj(x[n-1])).

@@ -64,6 +64,22 @@ def _c64(x) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.complex64).reshape(-1)
 
 
+def _ci16_host(x) -> np.ndarray | None:
+    """Interleaved complex int16 (N x 2 int16 numpy array) as a contiguous
+    array, else None."""
+    if isinstance(x, np.ndarray) and x.dtype == np.int16 and x.ndim == 2 and x.shape[-1] == 2:
+        return np.ascontiguousarray(x)
+    return None
+
+
+def _ci16_dev(x):
+    """A CUDA int16 tensor of shape (N, 2) (interleaved I, Q), else None."""
+    torch = _torch()
+    if x.dtype == torch.int16 and x.dim() == 2 and x.shape[-1] == 2:
+        return x.contiguous()
+    return None
+
+
 def _ptr(a: np.ndarray):
     return C.c_void_p(a.ctypes.data) if a.size else C.c_void_p(0)
 
@@ -232,8 +248,22 @@ class MultiRateChannelizerCuda(_Handle):
         _capi.call("fdsp_channelizer_reset", self._h)
 
     def apply(self, x, out=None, stream: int | None = None):
+        """Complex64 input, or complex int16 (N x 2 int16, converted on the
+        GPU inside the first kernel); one complex64 output per channel."""
         if _is_tensor(x):
+            x16 = _ci16_dev(x)
+            if x16 is not None:
+                return self._apply_ci16_device(x16, out, stream)
             return self._apply_device(x, out, stream)
+        x16 = _ci16_host(x)
+        if x16 is not None:
+            cnt = self.out_count(x16.shape[0])
+            outs = [np.empty(max(c, 1), np.complex64) for c in cnt]
+            optr = (C.c_void_p * self.num_channels)(*[o.ctypes.data for o in outs])
+            n_out = (C.c_uint64 * self.num_channels)()
+            _capi.call("fdsp_channelizer_apply_ci16_host", self._h, _ptr(x16), x16.shape[0], optr, None, n_out,
+                       C.c_void_p(stream or 0))
+            return [o[: n_out[i]] for i, o in enumerate(outs)]
         x = _c64(x)
         cnt = self.out_count(x.size)
         outs = [np.empty(max(c, 1), np.complex64) for c in cnt]
@@ -242,6 +272,18 @@ class MultiRateChannelizerCuda(_Handle):
         _capi.call("fdsp_channelizer_apply_host", self._h, _ptr(x), x.size, optr, None, n_out,
                    C.c_void_p(stream or 0))
         return [o[: n_out[i]] for i, o in enumerate(outs)]
+
+    def _apply_ci16_device(self, x16, out, stream):
+        torch = _torch()
+        n = x16.shape[0]
+        if out is None:
+            out = [torch.empty(max(c, 1), dtype=torch.complex64, device=x16.device) for c in self.out_count(n)]
+        optr = (C.c_void_p * self.num_channels)(*[o.data_ptr() for o in out])
+        cap = (C.c_uint64 * self.num_channels)(*[o.numel() for o in out])
+        n_out = (C.c_uint64 * self.num_channels)()
+        s = _stream_handle() if stream is None else stream
+        _capi.call("fdsp_channelizer_apply_ci16", self._h, _tptr(x16), n, optr, cap, n_out, C.c_void_p(s))
+        return [o[: n_out[i]] for i, o in enumerate(out)]
 
     def _apply_device(self, x, out, stream):
         torch = _torch()
@@ -317,14 +359,16 @@ class PolyphaseResamplerCuda(_Handle):
     def apply(self, x, out=None, stream: int | None = None):
         if _is_tensor(x):
             torch = _torch()
-            x = _dev_c64(x)
-            n = self.out_count(x.numel())
+            x16 = _ci16_dev(x)
+            fn = "fdsp_resampler_apply_ci16" if x16 is not None else "fdsp_resampler_apply"
+            x = x16 if x16 is not None else _dev_c64(x)
+            n_in = x.shape[0] if x16 is not None else x.numel()
+            n = self.out_count(n_in)
             if out is None:
                 out = torch.empty(max(n, 1), dtype=torch.complex64, device=x.device)
             got = C.c_uint64()
             s = _stream_handle() if stream is None else stream
-            _capi.call("fdsp_resampler_apply", self._h, _tptr(x), x.numel(), _tptr(out), out.numel(),
-                       C.byref(got), C.c_void_p(s))
+            _capi.call(fn, self._h, _tptr(x), n_in, _tptr(out), out.numel(), C.byref(got), C.c_void_p(s))
             return out[: got.value]
         real_in = np.isrealobj(x) and np.asarray(x).dtype != np.int16
         xa = _c64(x)
@@ -368,6 +412,28 @@ class FreqShiftCuda(_Handle):
         return v.value
 
     def apply(self, x, out=None, stream: int | None = None):
+        """Complex64 in and out, or (the int16 overload) complex int16 (N x 2
+        int16) in and out, converted on load and truncated on store."""
+        if _is_tensor(x) and _ci16_dev(x) is not None:
+            torch = _torch()
+            x16 = _ci16_dev(x)
+            n = x16.shape[0]
+            if out is None:
+                out = [torch.empty((max(n, 1), 2), dtype=torch.int16, device=x16.device)
+                       for _ in range(self.num_channels)]
+            optr = (C.c_void_p * self.num_channels)(*[o.data_ptr() for o in out])
+            s = _stream_handle() if stream is None else stream
+            _capi.call("fdsp_freq_shift_apply_ci16", self._h, _tptr(x16), n, optr, C.c_void_p(s))
+            res = [o[:n] for o in out]
+            return res[0] if self.single else res
+        if not _is_tensor(x) and _ci16_host(x) is not None:
+            x16 = _ci16_host(x)
+            n = x16.shape[0]
+            res = [np.empty((max(n, 1), 2), np.int16) for _ in range(self.num_channels)]
+            optr = (C.c_void_p * self.num_channels)(*[o.ctypes.data for o in res])
+            _capi.call("fdsp_freq_shift_apply_ci16_host", self._h, _ptr(x16), n, optr, C.c_void_p(stream or 0))
+            res = [o[:n] for o in res]
+            return res[0] if self.single else res
         if _is_tensor(x):
             torch = _torch()
             x = _dev_c64(x)
@@ -401,25 +467,34 @@ class FirFilterCuda(_Handle):
         _capi.call("fdsp_fir_reset", self._h)
 
     def apply(self, x, out=None, stream: int | None = None):
+        """Complex64 in and out, or (the int16 overload, fir_filter.cc:151-175)
+        complex int16 (N x 2 int16) in and out: converted inside the filter
+        kernel, truncated toward zero on the way out."""
         if _is_tensor(x):
             torch = _torch()
+            x16 = _ci16_dev(x)
+            s = _stream_handle() if stream is None else stream
+            if x16 is not None:
+                n = x16.shape[0]
+                if out is None:
+                    out = torch.empty((max(n, 1), 2), dtype=torch.int16, device=x16.device)
+                _capi.call("fdsp_fir_apply_ci16", self._h, _tptr(x16), n, _tptr(out), C.c_void_p(s))
+                return out[:n]
             x = _dev_c64(x)
             if out is None:
                 out = torch.empty(max(x.numel(), 1), dtype=torch.complex64, device=x.device)
-            s = _stream_handle() if stream is None else stream
             _capi.call("fdsp_fir_apply", self._h, _tptr(x), x.numel(), _tptr(out), C.c_void_p(s))
             return out[: x.numel()]
-        as_i16 = np.asarray(x).dtype == np.int16
+        x16 = _ci16_host(x)
+        if x16 is not None:
+            n = x16.shape[0]
+            out16 = np.empty((max(n, 1), 2), np.int16)
+            _capi.call("fdsp_fir_apply_ci16_host", self._h, _ptr(x16), n, _ptr(out16), C.c_void_p(stream or 0))
+            return out16[:n]
         xa = _c64(x)
         y = np.empty(max(xa.size, 1), np.complex64)
         _capi.call("fdsp_fir_apply_host", self._h, _ptr(xa), xa.size, _ptr(y), C.c_void_p(stream or 0))
-        y = y[: xa.size]
-        if as_i16:  # apply(vector<complex<int16_t>>): truncating cast back (fir_filter.cc:168-172)
-            out16 = np.empty((y.size, 2), np.int16)
-            out16[:, 0] = np.trunc(y.real).astype(np.int16)
-            out16[:, 1] = np.trunc(y.imag).astype(np.int16)
-            return out16
-        return y
+        return y[: xa.size]
 
 
 class PolarDiscriminatorCuda(_Handle):

@@ -75,6 +75,13 @@ SIGNATURES = {
     "fdsp_channelizer_apply": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
     "fdsp_channelizer_apply_host": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
     "fdsp_channelizer_kernel_launches": [_vp, _pu32],
+    "fdsp_channelizer_apply_ci16": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
+    "fdsp_channelizer_apply_ci16_host": [_vp, _vp, _u64, _pp, _pu64, _pu64, _vp],
+    "fdsp_resampler_apply_ci16": [_vp, _vp, _u64, _vp, _u64, _pu64, _vp],
+    "fdsp_freq_shift_apply_ci16": [_vp, _vp, _u64, _pp, _vp],
+    "fdsp_freq_shift_apply_ci16_host": [_vp, _vp, _u64, _pp, _vp],
+    "fdsp_fir_apply_ci16": [_vp, _vp, _u64, _vp, _vp],
+    "fdsp_fir_apply_ci16_host": [_vp, _vp, _u64, _vp, _vp],
     "fdsp_channelizer_tc_groups": [_vp, _pu32],
     "fdsp_server_create": [_u64, _u32, _pp],
     "fdsp_server_destroy": [_vp],

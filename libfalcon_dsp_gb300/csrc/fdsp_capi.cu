@@ -204,6 +204,12 @@ int fdsp_channelizer_apply(fdsp_channelizer* h, const fdsp_cf32* d_in, uint64_t 
                       n_out, (cudaStream_t)stream);
 }
 
+int fdsp_channelizer_apply_ci16(fdsp_channelizer* h, const int16_t* d_in, uint64_t n_in, fdsp_cf32* const* d_out,
+                                const uint64_t* out_cap, uint64_t* n_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return h->eng.apply_ci16(d_in, n_in, reinterpret_cast<float2* const*>(d_out), out_cap, n_out, (cudaStream_t)stream);
+}
+
 int fdsp_channelizer_set_precision(fdsp_channelizer* h, int precision) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
   return h->eng.set_precision(precision);
@@ -278,6 +284,35 @@ int fdsp_channelizer_apply_host(fdsp_channelizer* h, const fdsp_cf32* h_in, uint
   }
   if (n_in) FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * sizeof(float2), cudaMemcpyHostToDevice, s)));
   FDSP_TRY(h->eng.apply(static_cast<const float2*>(h->in.p), n_in, dptr.data(), nullptr, n_out, s));
+  for (uint32_t c = 0; c < nch; ++c) {
+    if (n_out[c])
+      FDSP_TRY(cuda_status(
+          cudaMemcpyAsync(h_out[c], dptr[c], n_out[c] * sizeof(float2), cudaMemcpyDeviceToHost, s)));
+  }
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+int fdsp_channelizer_apply_ci16_host(fdsp_channelizer* h, const int16_t* h_in, uint64_t n_in, fdsp_cf32* const* h_out,
+                                     const uint64_t* out_cap, uint64_t* n_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if ((n_in > 0 && !h_in) || !n_out) return FDSP_ERR_INVALID_ARG;
+  const uint32_t nch = h->eng.num_channels();
+  std::vector<uint64_t> cnt(nch);
+  FDSP_TRY(h->eng.out_counts(n_in, cnt.data()));
+  for (uint32_t c = 0; c < nch; ++c) {
+    if (out_cap && out_cap[c] < cnt[c]) return FDSP_ERR_CAPACITY;
+    if (cnt[c] > 0 && (!h_out || !h_out[c])) return FDSP_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  FDSP_TRY(h->in.ensure(n_in * 2 * sizeof(int16_t) + 16));
+  std::vector<float2*> dptr(nch);
+  for (uint32_t c = 0; c < nch; ++c) {
+    FDSP_TRY(h->out[c].ensure(cnt[c] * sizeof(float2) + 16));
+    dptr[c] = static_cast<float2*>(h->out[c].p);
+  }
+  if (n_in)
+    FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * 2 * sizeof(int16_t), cudaMemcpyHostToDevice, s)));
+  FDSP_TRY(h->eng.apply_ci16(static_cast<const int16_t*>(h->in.p), n_in, dptr.data(), nullptr, n_out, s));
   for (uint32_t c = 0; c < nch; ++c) {
     if (n_out[c])
       FDSP_TRY(cuda_status(
@@ -363,6 +398,13 @@ int fdsp_resampler_apply(fdsp_resampler* h, const fdsp_cf32* d_in, uint64_t n_in
   return h->eng.apply(reinterpret_cast<const float2*>(d_in), n_in, &o, &out_cap, n_out, (cudaStream_t)stream);
 }
 
+int fdsp_resampler_apply_ci16(fdsp_resampler* h, const int16_t* d_in, uint64_t n_in, fdsp_cf32* d_out,
+                              uint64_t out_cap, uint64_t* n_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  float2* o = reinterpret_cast<float2*>(d_out);
+  return h->eng.apply_ci16(d_in, n_in, &o, &out_cap, n_out, (cudaStream_t)stream);
+}
+
 int fdsp_resampler_apply_host(fdsp_resampler* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* h_out,
                               uint64_t out_cap, uint64_t* n_out, fdsp_stream_t stream) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
@@ -438,6 +480,31 @@ int fdsp_fir_apply_host(fdsp_fir* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_
   return cuda_status(cudaStreamSynchronize(s));
 }
 
+int fdsp_fir_apply_ci16(fdsp_fir* h, const int16_t* d_in, uint64_t n_in, int16_t* d_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (n_in == 0) return FDSP_OK;
+  if (!d_in || !d_out) return FDSP_ERR_INVALID_ARG;
+  FDSP_TRY(h->out.ensure(n_in * sizeof(float2) + 16));
+  float2* o = static_cast<float2*>(h->out.p);
+  uint64_t cnt = 0;
+  FDSP_TRY(h->eng.apply_ci16(d_in, n_in, &o, nullptr, &cnt, (cudaStream_t)stream));
+  return launch_cf32_to_ci16(o, (int64_t)cnt, reinterpret_cast<short2*>(d_out), (cudaStream_t)stream);
+}
+
+int fdsp_fir_apply_ci16_host(fdsp_fir* h, const int16_t* h_in, uint64_t n_in, int16_t* h_out, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (n_in == 0) return FDSP_OK;
+  if (!h_in || !h_out) return FDSP_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  FDSP_TRY(h->in.ensure(n_in * 4 * sizeof(int16_t) + 16));  // int16 input, then int16 output
+  int16_t* din = static_cast<int16_t*>(h->in.p);
+  int16_t* dout = din + 2 * n_in;
+  FDSP_TRY(cuda_status(cudaMemcpyAsync(din, h_in, n_in * 2 * sizeof(int16_t), cudaMemcpyHostToDevice, s)));
+  FDSP_TRY(fdsp_fir_apply_ci16(h, din, n_in, dout, stream));
+  FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out, dout, n_in * 2 * sizeof(int16_t), cudaMemcpyDeviceToHost, s)));
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
 /* ---------------- frequency shift ---------------- */
 int fdsp_freq_shift_create(uint32_t fs, const int32_t* shifts, uint32_t nch, fdsp_freq_shift** out) {
   if (!out) return FDSP_ERR_INVALID_ARG;
@@ -507,6 +574,49 @@ int fdsp_freq_shift_apply(fdsp_freq_shift* h, const fdsp_cf32* d_in, uint64_t n_
   FDSP_TRY(launch_freq_shift(L, (cudaStream_t)stream));
   h->abs0 += n_in;
   return FDSP_OK;
+}
+
+int fdsp_freq_shift_apply_ci16(fdsp_freq_shift* h, const int16_t* d_in, uint64_t n_in, int16_t* const* d_out,
+                               fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (n_in == 0) return FDSP_OK;
+  if (!d_in || !d_out) return FDSP_ERR_INVALID_ARG;
+  static thread_local ShiftLaunch L;
+  std::memset(&L, 0, sizeof(L));
+  L.in = reinterpret_cast<const float2*>(d_in);
+  L.i16 = 1;
+  L.N = (int64_t)n_in;
+  L.nch = (int32_t)h->nco.size();
+  L.nco = h->d_nco;
+  for (size_t c = 0; c < h->nco.size(); ++c) {
+    if (!d_out[c]) return FDSP_ERR_INVALID_ARG;
+    L.out[c] = reinterpret_cast<float2*>(d_out[c]);
+    const uint32_t R = h->nco[c].rollover;
+    L.nco_base[c] = R ? (uint32_t)(h->abs0 % R) : 0u;
+  }
+  FDSP_TRY(launch_freq_shift(L, (cudaStream_t)stream));
+  h->abs0 += n_in;
+  return FDSP_OK;
+}
+
+int fdsp_freq_shift_apply_ci16_host(fdsp_freq_shift* h, const int16_t* h_in, uint64_t n_in, int16_t* const* h_out,
+                                    fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (n_in == 0) return FDSP_OK;
+  if (!h_in || !h_out) return FDSP_ERR_INVALID_ARG;
+  const size_t nch = h->nco.size();
+  cudaStream_t s = (cudaStream_t)stream;
+  FDSP_TRY(h->in.ensure(n_in * 2 * sizeof(int16_t) + 16));
+  std::vector<int16_t*> d(nch);
+  for (size_t c = 0; c < nch; ++c) {
+    FDSP_TRY(h->out[c].ensure(n_in * 2 * sizeof(int16_t) + 16));
+    d[c] = static_cast<int16_t*>(h->out[c].p);
+  }
+  FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * 2 * sizeof(int16_t), cudaMemcpyHostToDevice, s)));
+  FDSP_TRY(fdsp_freq_shift_apply_ci16(h, static_cast<const int16_t*>(h->in.p), n_in, d.data(), stream));
+  for (size_t c = 0; c < nch; ++c)
+    FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out[c], d[c], n_in * 2 * sizeof(int16_t), cudaMemcpyDeviceToHost, s)));
+  return cuda_status(cudaStreamSynchronize(s));
 }
 
 int fdsp_freq_shift_apply_host(fdsp_freq_shift* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* const* h_out,

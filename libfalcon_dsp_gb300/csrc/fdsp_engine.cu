@@ -202,6 +202,12 @@ __global__ void __launch_bounds__(kThreads, 3) poly_fp32_kernel(const __grid_con
     const int64_t v = sb + t;
     const float2* src = L.block;
     uint32_t bytes = 0;
+    const int q = t / D;
+    if (L.block16 != nullptr && v >= 0 && v < L.N) {  // int16 front end: convert on the way in
+      const short2 s = L.block16[v];
+      xs[(t - q * D) * P + q] = make_float2((float)s.x, (float)s.y);
+      continue;
+    }
     if (v < 0) {
       const int64_t hv = v + L.H;
       if (hv >= 0) {
@@ -212,7 +218,6 @@ __global__ void __launch_bounds__(kThreads, 3) poly_fp32_kernel(const __grid_con
       src = L.block + v;
       bytes = 8;
     }
-    const int q = t / D;
     const uint32_t dst = (uint32_t)__cvta_generic_to_shared(xs + (t - q * D) * P + q);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
   }
@@ -270,12 +275,19 @@ __global__ void __launch_bounds__(kThreads, 3) poly_fp32_kernel(const __grid_con
 }
 
 // History after a block: the last H samples of [old history | block].
-__global__ void hist_update_kernel(const float2* __restrict__ old_hist, const float2* __restrict__ block, int64_t N,
-                                   int H, float2* __restrict__ new_hist) {
+__global__ void hist_update_kernel(const float2* __restrict__ old_hist, const float2* __restrict__ block,
+                                   const short2* __restrict__ block16, int64_t N, int H, float2* __restrict__ new_hist) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= H) return;
   const int64_t v = N + i;
-  new_hist[i] = v < H ? old_hist[v] : block[v - H];
+  if (v < H) {
+    new_hist[i] = old_hist[v];
+  } else if (block16 != nullptr) {
+    const short2 s = block16[v - H];
+    new_hist[i] = make_float2((float)s.x, (float)s.y);
+  } else {
+    new_hist[i] = block[v - H];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -628,7 +640,8 @@ template <int NB>
 int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream) {
   static thread_local PolyLaunch<NB> L;  // ~20 KB: keep it off the stack
   std::memset(&L, 0, sizeof(L));
-  L.block = d_in;
+  L.block = in16_ ? nullptr : d_in;
+  L.block16 = in16_;
   L.hist = d_hist_[hist_cur_];
   L.N = (int64_t)n;
   L.H = H_;
@@ -795,14 +808,23 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
     }
   }
   if (H_ > 0) {
-    hist_update_kernel<<<(H_ + 255) / 256, 256, 0, stream>>>(d_hist_[hist_cur_], d_in, (int64_t)n, H_,
-                                                              d_hist_[hist_cur_ ^ 1]);
+    hist_update_kernel<<<(H_ + 255) / 256, 256, 0, stream>>>(d_hist_[hist_cur_], in16_ ? nullptr : d_in, in16_,
+                                                              (int64_t)n, H_, d_hist_[hist_cur_ ^ 1]);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     hist_cur_ ^= 1;
     launches_last_++;
   }
   return FDSP_OK;
+}
+
+int PolyEngine::apply_ci16(const int16_t* d_in, uint64_t n, float2* const* out, const uint64_t* cap,
+                           uint64_t* n_out, cudaStream_t stream) {
+  in16_ = reinterpret_cast<const short2*>(d_in);
+  // the float pointer is only checked for NULL; every kernel reads in16_
+  const int st = apply(reinterpret_cast<const float2*>(d_in), n, out, cap, n_out, stream);
+  in16_ = nullptr;
+  return st;
 }
 
 int PolyEngine::apply(const float2* d_in, uint64_t n, float2* const* out, const uint64_t* cap, uint64_t* n_out,

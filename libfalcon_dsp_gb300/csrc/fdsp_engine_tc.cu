@@ -93,7 +93,12 @@ __device__ __forceinline__ float2 load_x(const TcLaunch& L, int64_t v) {
     const int64_t hv = v + L.H;
     return hv >= 0 ? L.hist[hv] : make_float2(0.f, 0.f);
   }
-  return v < L.N ? __ldg(L.block + v) : make_float2(0.f, 0.f);
+  if (v >= L.N) return make_float2(0.f, 0.f);
+  if (L.block16 != nullptr) {
+    const short2 s = L.block16[v];
+    return make_float2((float)s.x, (float)s.y);
+  }
+  return __ldg(L.block + v);
 }
 
 template <int FMT>
@@ -116,11 +121,19 @@ __device__ __forceinline__ void split2(float2 x, uint32_t& hi, uint32_t& lo) {
 // [history | block] -> packed {hi, lo} 16-bit pairs, once per apply: every
 // sample is used by many windows, so the split is not repeated per use.
 template <int FMT>
-__global__ void split_input_kernel(const float2* __restrict__ block, const float2* __restrict__ hist, int64_t N,
-                                   int H, uint2* __restrict__ xhl) {
+__global__ void split_input_kernel(const float2* __restrict__ block, const short2* __restrict__ block16,
+                                   const float2* __restrict__ hist, int64_t N, int H, uint2* __restrict__ xhl) {
   const int64_t total = N + H;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
-    const float2 x = u < H ? hist[u] : block[u - H];
+    float2 x;
+    if (u < H) {
+      x = hist[u];
+    } else if (block16 != nullptr) {  // int16 front end
+      const short2 s = block16[u - H];
+      x = make_float2((float)s.x, (float)s.y);
+    } else {
+      x = block[u - H];
+    }
     uint2 hl;
     split2<FMT>(x, hl.x, hl.y);
     xhl[u] = hl;
@@ -706,9 +719,11 @@ int PolyEngine::prepare_tc_input(const float2* d_in, uint64_t n, cudaStream_t st
   }
   const int64_t blocks = std::min<int64_t>((int64_t)(need + 255) / 256, (int64_t)num_sms_ * 8);
   if (tc_fmt_ == 0)
-    split_input_kernel<0><<<(unsigned)blocks, 256, 0, stream>>>(d_in, d_hist_[hist_cur_], (int64_t)n, H_, d_xhl_);
+    split_input_kernel<0><<<(unsigned)blocks, 256, 0, stream>>>(in16_ ? nullptr : d_in, in16_, d_hist_[hist_cur_],
+                                                                 (int64_t)n, H_, d_xhl_);
   else
-    split_input_kernel<1><<<(unsigned)blocks, 256, 0, stream>>>(d_in, d_hist_[hist_cur_], (int64_t)n, H_, d_xhl_);
+    split_input_kernel<1><<<(unsigned)blocks, 256, 0, stream>>>(in16_ ? nullptr : d_in, in16_, d_hist_[hist_cur_],
+                                                                 (int64_t)n, H_, d_xhl_);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e);
   launches_last_++;
@@ -883,7 +898,8 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
   static thread_local TcLaunch L;
   for (const auto& p : plans) {
     std::memset(&L, 0, sizeof(L));
-    L.block = d_in;
+    L.block = in16_ ? nullptr : d_in;
+    L.block16 = in16_;
     L.hist = d_hist_[hist_cur_];
     L.xhl = d_xhl_;
     L.nco = d_nco_;

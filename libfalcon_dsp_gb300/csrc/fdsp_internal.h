@@ -79,6 +79,7 @@ struct WorkSet {
 template <int NB>
 struct PolyLaunch {
   const float2* block;      // device input block (N samples)
+  const short2* block16;    // or, when set, the block as complex int16 (converted on load)
   const float2* hist;       // device history (H samples preceding block)
   int64_t N;
   int32_t H;
@@ -148,6 +149,7 @@ struct TcSlotHot {
 
 struct TcLaunch {
   const float2* block;
+  const short2* block16;             // or, when set, the block as complex int16
   const float2* hist;
   const uint2* xhl;                  // [history | block] as packed {hi, lo} 16-bit pairs
   const NcoConst* nco;
@@ -264,6 +266,11 @@ class PolyEngine {
   int out_counts(uint64_t n_in, uint64_t* n_out) const;
   // Enqueue one streaming block on `stream`; outputs of channel c go to out[c]
   // (device pointers, capacity checked against cap[c] when cap != nullptr).
+  // complex int16 input, converted to float inside the first kernel that
+  // reads it (the staging of the FP32 kernel, the {hi, lo} split of the
+  // tensor-core path, the history update)
+  int apply_ci16(const int16_t* d_in, uint64_t n, float2* const* out, const uint64_t* cap, uint64_t* n_out,
+                 cudaStream_t stream);
   int apply(const float2* d_in, uint64_t n, float2* const* out, const uint64_t* cap, uint64_t* n_out,
             cudaStream_t stream);
   void reset();
@@ -334,6 +341,7 @@ class PolyEngine {
   NcoConst* d_nco_ = nullptr;
   float2* d_hist_[2] = {nullptr, nullptr};
   int hist_cur_ = 0;
+  const short2* in16_ = nullptr;  // set for the duration of apply_ci16
   uint64_t abs0_ = 0;               // samples since reset at the next block
   int launches_last_ = 0;
   int tc_groups_last_ = 0;

@@ -37,7 +37,12 @@ __global__ void __launch_bounds__(kShiftThreads)
 #pragma unroll
   for (int u = 0; u < kShiftPer; ++u) {
     const int64_t i = t0 + threadIdx.x + (int64_t)u * kShiftThreads;
-    x[u] = i < L.N ? L.in[i] : make_float2(0.f, 0.f);
+    if (L.i16) {
+      const short2 s = i < L.N ? reinterpret_cast<const short2*>(L.in)[i] : make_short2(0, 0);
+      x[u] = make_float2((float)s.x, (float)s.y);
+    } else {
+      x[u] = i < L.N ? L.in[i] : make_float2(0.f, 0.f);
+    }
   }
   for (int c = 0; c < L.nch; ++c) {
     const NcoConst nc = L.nco[c];
@@ -46,7 +51,11 @@ __global__ void __launch_bounds__(kShiftThreads)
 #pragma unroll
       for (int u = 0; u < kShiftPer; ++u) {
         const int64_t i = t0 + threadIdx.x + (int64_t)u * kShiftThreads;
-        if (i < L.N) out[i] = x[u];
+        if (i >= L.N) continue;
+        if (L.i16)
+          reinterpret_cast<short2*>(out)[i] = make_short2((short)__float2int_rz(x[u].x), (short)__float2int_rz(x[u].y));
+        else
+          out[i] = x[u];
       }
       continue;
     }
@@ -60,7 +69,11 @@ __global__ void __launch_bounds__(kShiftThreads)
       const float2 e = phasor64_sp(p * nc.omega64);
       if (i < L.N) {
         const float2 v = x[u];
-        out[i] = make_float2(fmaf(v.x, e.x, -v.y * e.y), fmaf(v.x, e.y, v.y * e.x));
+        const float2 y = make_float2(fmaf(v.x, e.x, -v.y * e.y), fmaf(v.x, e.y, v.y * e.x));
+        if (L.i16)
+          reinterpret_cast<short2*>(out)[i] = make_short2((short)__float2int_rz(y.x), (short)__float2int_rz(y.y));
+        else
+          out[i] = y;
       }
       p += step;
       if (p >= R) p -= R;
@@ -73,6 +86,20 @@ int launch_freq_shift(const ShiftLaunch& L, cudaStream_t stream) {
   const int64_t nblocks = (L.N + kShiftTile - 1) / kShiftTile;
   if (nblocks > 0x7fffffffLL) return FDSP_ERR_UNSUPPORTED;
   freq_shift_kernel<<<(unsigned)nblocks, kShiftThreads, 0, stream>>>(L);
+  return cuda_status(cudaGetLastError());
+}
+
+__global__ void cf32_to_ci16_kernel(const float2* __restrict__ in, int64_t n, short2* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = in[i];
+    out[i] = make_short2((short)__float2int_rz(v.x), (short)__float2int_rz(v.y));
+  }
+}
+
+int launch_cf32_to_ci16(const float2* in, int64_t n, short2* out, cudaStream_t stream) {
+  if (n <= 0) return FDSP_OK;
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
+  cf32_to_ci16_kernel<<<(unsigned)blocks, 256, 0, stream>>>(in, n, out);
   return cuda_status(cudaGetLastError());
 }
 
