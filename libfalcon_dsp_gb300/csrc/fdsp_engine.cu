@@ -198,28 +198,41 @@ __global__ void __launch_bounds__(kThreads, 3) poly_fp32_kernel(const __grid_con
   // copies (every copy of the tile in flight at once).  Negative indices come
   // from the history (the H samples before the block); past the block end the
   // copy reads 0 bytes and zero-fills.
-  for (int t = threadIdx.x; t < len; t += blockDim.x) {
-    const int64_t v = sb + t;
-    const float2* src = L.block;
-    uint32_t bytes = 0;
-    const int q = t / D;
-    if (L.block16 != nullptr && v >= 0 && v < L.N) {  // int16 front end: convert on the way in
-      const short2 s = L.block16[v];
-      xs[(t - q * D) * P + q] = make_float2((float)s.x, (float)s.y);
-      continue;
-    }
-    if (v < 0) {
-      const int64_t hv = v + L.H;
-      if (hv >= 0) {
-        src = L.hist + hv;
+  if (L.block16 == nullptr) {
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+      const int64_t v = sb + t;
+      const float2* src = L.block;
+      uint32_t bytes = 0;
+      if (v < 0) {
+        const int64_t hv = v + L.H;
+        if (hv >= 0) {
+          src = L.hist + hv;
+          bytes = 8;
+        }
+      } else if (v < L.N) {
+        src = L.block + v;
         bytes = 8;
       }
-    } else if (v < L.N) {
-      src = L.block + v;
-      bytes = 8;
+      const int q = t / D;
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(xs + (t - q * D) * P + q);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
     }
-    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(xs + (t - q * D) * P + q);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+  } else {
+    // int16 front end: block samples are converted on the way in (the
+    // history is already float)
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+      const int64_t v = sb + t;
+      const int q = t / D;
+      float2 x = make_float2(0.f, 0.f);
+      if (v < 0) {
+        const int64_t hv = v + L.H;
+        if (hv >= 0) x = L.hist[hv];
+      } else if (v < L.N) {
+        const short2 s = L.block16[v];
+        x = make_float2((float)s.x, (float)s.y);
+      }
+      xs[(t - q * D) * P + q] = x;
+    }
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
   // Stage the taps of every work set (when they fit) and the per-channel NCO
