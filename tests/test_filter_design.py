@@ -105,3 +105,21 @@ def test_native_designer_any_rate():
     ref64 = FD.kaiser_firls_lowpass(301, 147, 160, beta=8.6)
     assert np.max(np.abs(g.real - ref64)) <= 1e-6 * np.max(np.abs(ref64))
     assert FD.up_down(48000, 44100) == (147, 160)
+
+
+def test_iq_files_round_trip(tmp_path):
+    from libfalcon_dsp_gb300 import iq_files as IQ
+    rng = np.random.default_rng(9)
+    x16 = rng.integers(-32768, 32768, size=(1001, 2)).astype(np.int16)
+    xc = (rng.standard_normal(77) + 1j * rng.standard_normal(77)).astype(np.complex64)
+    for t in (IQ.BINARY, IQ.ASCII):
+        p = str(tmp_path / f"a{t}")
+        assert IQ.write_complex_data_to_file(p, t, x16)
+        assert np.array_equal(IQ.read_complex_data_from_file(p, t), x16)
+        p = str(tmp_path / f"b{t}")
+        assert IQ.write_complex_data_to_file(p, t, xc)
+        assert np.array_equal(IQ.read_complex_data_from_file(p, t, dtype=np.float32), xc)
+    # BINARY int16 is little-endian "<2h" pairs
+    raw = np.fromfile(str(tmp_path / "a0"), dtype="<i2").reshape(-1, 2)
+    assert np.array_equal(raw, x16)
+    assert IQ.read_complex_data_from_file(str(tmp_path / "missing"), IQ.BINARY) is None
