@@ -325,6 +325,13 @@ int fdsp_fir_destroy(fdsp_fir *h);
 int fdsp_fir_reset(fdsp_fir *h);
 int fdsp_fir_apply(fdsp_fir *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *d_out, fdsp_stream_t stream);
 int fdsp_fir_apply_host(fdsp_fir *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *h_out, fdsp_stream_t stream);
+/* FDSP_PRECISION_FP32 (default) or the tensor-core split-precision forms
+ * FDSP_PRECISION_FP16X3 / FDSP_PRECISION_BF16X3: the FIR as a Toeplitz
+ * product on tcgen05 (32 consecutive outputs per row of the tile), for up to
+ * 64 taps (longer filters keep the FP32 kernel).  Resets the streaming state. */
+int fdsp_fir_set_precision(fdsp_fir *h, int precision);
+/* 1 when the last apply ran on the tensor-core kernel, else 0 */
+int fdsp_fir_tc_groups(const fdsp_fir *h, uint32_t *n);
 /* int16 overload (src/transform/falcon_dsp_fir_filter.cc:151-175): complex
  * int16 in (converted inside the filter kernel), complex int16 out
  * (truncated toward zero). */

@@ -466,6 +466,17 @@ class FirFilterCuda(_Handle):
     def reset_state(self) -> None:
         _capi.call("fdsp_fir_reset", self._h)
 
+    def set_precision(self, mode: str = "fp32") -> None:
+        """'fp32' (default) or the tensor-core forms 'fp16x3' / 'bf16x3'
+        (Toeplitz product, (hi+lo)(hi+lo), FP32 accumulation; up to 64 taps).
+        Resets the streaming state."""
+        _capi.call("fdsp_fir_set_precision", self._h, MultiRateChannelizerCuda.PRECISION[mode])
+
+    def tc_groups(self) -> int:
+        v = C.c_uint32()
+        _capi.call("fdsp_fir_tc_groups", self._h, C.byref(v))
+        return v.value
+
     def apply(self, x, out=None, stream: int | None = None):
         """Complex64 in and out, or (the int16 overload, fir_filter.cc:151-175)
         complex int16 (N x 2 int16) in and out: converted inside the filter

@@ -81,6 +81,8 @@ SIGNATURES = {
     "fdsp_freq_shift_apply_ci16": [_vp, _vp, _u64, _pp, _vp],
     "fdsp_freq_shift_apply_ci16_host": [_vp, _vp, _u64, _pp, _vp],
     "fdsp_fir_apply_ci16": [_vp, _vp, _u64, _vp, _vp],
+    "fdsp_fir_set_precision": [_vp, C.c_int],
+    "fdsp_fir_tc_groups": [_vp, _pu32],
     "fdsp_fir_apply_ci16_host": [_vp, _vp, _u64, _vp, _vp],
     "fdsp_channelizer_tc_groups": [_vp, _pu32],
     "fdsp_server_create": [_u64, _u32, _pp],

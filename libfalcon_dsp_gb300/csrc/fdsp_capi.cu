@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <vector>
 
@@ -41,8 +42,11 @@ struct fdsp_resampler {
 };
 
 struct fdsp_fir {
-  PolyEngine eng;
+  PolyEngine eng;                   // y[n] = sum_k h[k] x[n-k]: one channel, up = down = 1
+  std::unique_ptr<PolyEngine> toe;  // tensor-core precisions: the Toeplitz form below
+  std::vector<fdsp_cf32> taps;
   DevBuf in, out;
+  PolyEngine& active() { return toe ? *toe : eng; }
 };
 
 struct fdsp_freq_shift {
@@ -443,7 +447,50 @@ int fdsp_fir_create(const fdsp_cf32* coeffs, uint32_t ncoeffs, fdsp_fir** out) {
     delete h;
     return st;
   }
+  h->taps.assign(coeffs, coeffs + ncoeffs);
   *out = h;
+  return FDSP_OK;
+}
+
+// Tensor-core FIR.  The filter equals a resampler with up = down = L and the
+// taps spread L apart (h[k] at k L, zeros between): every output then uses
+// tap phase 0, and the engine splits the outputs into L interleaved lanes
+// (output m = r + L j, r < L) that read the input r samples apart.  On the
+// tensor-core kernel those L lanes are the columns of one merge set: a
+// Toeplitz product, with the input tile read once for L outputs a row.
+constexpr uint32_t kFirToeplitzLanes = 32;
+
+int fdsp_fir_set_precision(fdsp_fir* h, int precision) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (precision == FDSP_PRECISION_FP32) {
+    h->toe.reset();
+    h->eng.reset();
+    return FDSP_OK;
+  }
+  if (precision != FDSP_PRECISION_FP16X3 && precision != FDSP_PRECISION_BF16X3) return FDSP_ERR_INVALID_ARG;
+  const uint32_t L = kFirToeplitzLanes;
+  std::vector<fdsp_cf32> spread((size_t)h->taps.size() * L, fdsp_cf32{0.f, 0.f});
+  for (size_t k = 0; k < h->taps.size(); ++k) spread[k * L] = h->taps[k];
+  std::unique_ptr<PolyEngine> e(new (std::nothrow) PolyEngine());
+  if (!e) return FDSP_ERR_ALLOC;
+  fdsp_channel_cfg c;
+  c.output_sample_rate_in_sps = 0;
+  c.freq_shift_in_hz = 0;
+  c.up_rate = L;
+  c.down_rate = L;
+  c.resample_filter_coeffs = spread.data();
+  c.num_coeffs = (uint32_t)spread.size();
+  FDSP_TRY(e->init(1, &c, 1, true));
+  FDSP_TRY(e->set_precision(precision));
+  h->toe = std::move(e);
+  h->eng.reset();
+  return FDSP_OK;
+}
+
+int fdsp_fir_tc_groups(const fdsp_fir* h, uint32_t* n) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!n) return FDSP_ERR_INVALID_ARG;
+  *n = h->toe ? (uint32_t)h->toe->tc_groups_last() : 0u;
   return FDSP_OK;
 }
 
@@ -455,7 +502,7 @@ int fdsp_fir_destroy(fdsp_fir* h) {
 
 int fdsp_fir_reset(fdsp_fir* h) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
-  h->eng.reset();
+  h->active().reset();
   return FDSP_OK;
 }
 
@@ -463,7 +510,7 @@ int fdsp_fir_apply(fdsp_fir* h, const fdsp_cf32* d_in, uint64_t n_in, fdsp_cf32*
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
   float2* o = reinterpret_cast<float2*>(d_out);
   uint64_t cnt = 0;
-  return h->eng.apply(reinterpret_cast<const float2*>(d_in), n_in, &o, nullptr, &cnt, (cudaStream_t)stream);
+  return h->active().apply(reinterpret_cast<const float2*>(d_in), n_in, &o, nullptr, &cnt, (cudaStream_t)stream);
 }
 
 int fdsp_fir_apply_host(fdsp_fir* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* h_out, fdsp_stream_t stream) {
@@ -475,7 +522,7 @@ int fdsp_fir_apply_host(fdsp_fir* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_
   if (n_in) FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * sizeof(float2), cudaMemcpyHostToDevice, s)));
   float2* o = static_cast<float2*>(h->out.p);
   uint64_t cnt = 0;
-  FDSP_TRY(h->eng.apply(static_cast<const float2*>(h->in.p), n_in, &o, nullptr, &cnt, s));
+  FDSP_TRY(h->active().apply(static_cast<const float2*>(h->in.p), n_in, &o, nullptr, &cnt, s));
   if (cnt) FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out, o, cnt * sizeof(float2), cudaMemcpyDeviceToHost, s)));
   return cuda_status(cudaStreamSynchronize(s));
 }
@@ -487,7 +534,7 @@ int fdsp_fir_apply_ci16(fdsp_fir* h, const int16_t* d_in, uint64_t n_in, int16_t
   FDSP_TRY(h->out.ensure(n_in * sizeof(float2) + 16));
   float2* o = static_cast<float2*>(h->out.p);
   uint64_t cnt = 0;
-  FDSP_TRY(h->eng.apply_ci16(d_in, n_in, &o, nullptr, &cnt, (cudaStream_t)stream));
+  FDSP_TRY(h->active().apply_ci16(d_in, n_in, &o, nullptr, &cnt, (cudaStream_t)stream));
   return launch_cf32_to_ci16(o, (int64_t)cnt, reinterpret_cast<short2*>(d_out), (cudaStream_t)stream);
 }
 
