@@ -240,6 +240,27 @@ def other_configs(dev) -> dict:
     res["fir4095_dec10_fm"] = {"n_in": x.numel(), "n_audio": n_aud, "ms": round(ms, 3),
                                "value": round(x.numel() / ms / 1e3, 1), "unit": "input Msamples/s",
                                "audio_snr_db": round(snr, 2), "fir_gflops": round(4 * 4095 * (n_aud + 1) / ms / 1e6, 1)}
+    # standalone complex FIR, 64 complex taps at full rate, 2^26 samples: the
+    # FP32 kernel and the tensor-core Toeplitz form (fp16 hi+lo)
+    g = torch.Generator(device="cpu").manual_seed(2030)
+    hf = (torch.randn(64, dtype=torch.complex64, generator=g) * 0.1).numpy()
+    x = torch.randn(1 << 26, dtype=torch.complex64, device=dev) * 0.5
+    y = torch.empty_like(x)
+    fir = {"n_in": x.numel(), "taps": 64}
+    for mode in ("fp32", "fp16x3"):
+        f = F.FirFilterCuda(hf)
+        f.set_precision(mode)
+
+        def c6(f=f):
+            f.reset_state()
+            f.apply(x, out=y)
+            return x.numel()
+        ms, n = _time_device(c6, reps=3, warm=2)
+        fir[mode] = {"ms": round(ms, 3), "value": round(n / ms / 1e3, 1), "unit": "output Msamples/s",
+                     "tflops": round(8 * 64 * n / ms / 1e9, 2)}
+        if mode != "fp32":
+            fir[mode]["tensor_core"] = bool(f.tc_groups())
+    res["fir64_complex_2p26"] = fir
     return res
 
 
