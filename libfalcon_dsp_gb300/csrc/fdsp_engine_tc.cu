@@ -66,6 +66,7 @@ constexpr int kTcMaxTaps = 64;        // taps per phase of a chunk
 constexpr int kTcMaxKw = 128;         // taps of a merged window
 constexpr size_t kTcSmemMax = 225 * 1024;
 constexpr int kTcMaxBuf = 4;          // input buffers
+constexpr size_t kTcRawMax = 48 * 1024; // raw span buffer (bulk-copy staging) at most
 
 // Constants of one channel slot (Re/Im column pair) of a merge set, staged
 // in shared memory: read once per item (row-0 counter) and on the exact
@@ -155,6 +156,31 @@ __device__ __forceinline__ void stage_half(const TcLaunch& L, int64_t v, uint32_
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
 }
 
+// Bulk copy (one TMA transfer) of the {hi, lo} pairs of absolute samples
+// [u0, u0 + raw_span) that exist (0 <= u < N + H) into the raw buffer, whose
+// element i holds sample (u0 & ~1) + i; completion is counted on `bar`.  The
+// copy starts and ends on even samples (16-byte aligned; the scratch array
+// has one spare pair past its end); a span with no data only arrives.
+__device__ __forceinline__ void raw_issue(const TcLaunch& L, int64_t u0, uint32_t raw_s, uint64_t* bar) {
+  const int64_t total = L.N + L.H;
+  const int64_t base = u0 & ~1LL;
+  const int64_t c0 = (u0 < 0 ? 0 : u0) & ~1LL;
+  int64_t hi = u0 + L.raw_span;
+  if (hi > total) hi = total;
+  const int64_t c1 = (hi + 1) & ~1LL;
+  const uint32_t bar_s = tc::smem_u32(bar);
+  if (c1 > c0) {
+    const uint32_t bytes = (uint32_t)((c1 - c0) * 8);
+    const uint32_t dst = raw_s + (uint32_t)((c0 - base) * 8);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar_s), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                 "l"(L.xhl + c0), "r"(bytes), "r"(bar_s)
+                 : "memory");
+  } else {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar_s) : "memory");
+  }
+}
+
 // D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
 __device__ __forceinline__ void mma_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                        uint32_t accumulate) {
@@ -177,6 +203,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
   __shared__ __align__(8) uint64_t bar_d_full[kTcDSlots];    // accumulator ready  (commit)
   __shared__ __align__(8) uint64_t bar_d_empty[kTcDSlots];   // accumulator drained (one arrival per group warp)
   __shared__ __align__(8) uint64_t bar_b_full;               // B + slot constants (one arrival per producer warp)
+  __shared__ __align__(8) uint64_t bar_raw;                  // raw span landed    (bulk copy)
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane_id = tid & 31;
@@ -197,6 +224,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       tc::mbar_init(&bar_d_empty[i], 4);
     }
     tc::mbar_init(&bar_b_full, kTcProdThreads / 32);
+    tc::mbar_init(&bar_raw, 1);
     tc::mbar_fence_init();
   }
   tc::fence_before_sync();
@@ -207,20 +235,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
 
   if (warp < 3) {
     // ------------------------------------------------------------ producers
-    // B of every merge set: core (cg, k) comes from the work set that owns
-    // column group cg and tap k, else it is zero.
+    // B of every merge set: column pair s (slot s) of core row k comes from
+    // the work set that owns slot s and tap k (its channel i = s - s0 sits in
+    // column group i / 4, pair i % 4 of the chunk's packed B), else it is zero.
     for (int mi = 0; mi < nms; ++mi) {
       const TcMset& M = L.ms[mi];
       const int ncores = (M.N / 8) * M.Kw;
       for (int p = tid; p < ncores * 8; p += kTcProdThreads) {
         const int core = p >> 3, piece = p & 7;
         const int cg = core / M.Kw, k = core - cg * M.Kw;
+        const int slot = (cg * 8 + piece) >> 1, half = piece & 1;
         uint8_t* dst = smem + M.boff + (size_t)core * 128 + piece * 16;
         const uint8_t* src = nullptr;
         for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
           const TcWorkSet& W = L.ws[wi];
-          if (cg >= W.cg0 && cg < W.cg0 + W.ng && k >= W.o && k < W.o + W.T) {
-            src = W.b + ((size_t)(cg - W.cg0) * W.T + (k - W.o)) * 128 + piece * 16;
+          const int i = slot - W.s0;
+          if (i >= 0 && i < W.n && k >= W.o && k < W.o + W.T) {
+            src = W.b + ((size_t)(i >> 2) * W.T + (k - W.o)) * 128 + (2 * (i & 3) + half) * 16;
             break;
           }
         }
@@ -236,9 +267,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         sm.R = 0x7fffffffu;
         for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
           const TcWorkSet& W = L.ws[wi];
-          const int i = s - 4 * W.cg0;
-          if (i >= 0 && i < 4 * W.ng) {
-            if (i < W.n) {
+          const int i = s - W.s0;
+          if (i >= 0 && i < W.n) {
+            {
               const int c = W.ch[i];
               const NcoConst nc = L.nco[c];
               sm.nco.omega64 = nc.omega64;
@@ -280,6 +311,68 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     __syncwarp();
     if (lane_id == 0) tc::mbar_arrive(&bar_b_full);
 
+    if (L.raw_span > 0) {
+      // tiles through the raw buffer: one bulk copy brings the tile's whole
+      // input span; the three producer warps then write the records (v, q)
+      // (phase D = phase 0 one row on) from shared memory, phases fastest
+      // across threads (Qp is odd, so 8 consecutive records hit 8 distinct
+      // bank groups).  The next tile's copy is issued once the raw buffer
+      // has been read, so it overlaps the MMAs of this tile.
+      const uint32_t raw_s = tc::smem_u32(smem + L.raw_off);
+      const uint2* raw = reinterpret_cast<const uint2*>(smem + L.raw_off);
+      const int64_t total = L.N + L.H;
+      const int V = L.V, Qp = L.Qp, nbuf = L.nbuf;
+      const int nrec = V * Qp;
+      const int step_q = kTcProdThreads / V, step_v = kTcProdThreads % V;
+      bool pending = false;
+      if (tid == 0 && blockIdx.x < L.ntiles) raw_issue(L, (int64_t)blockIdx.x * 128 * D + L.B0 + L.H, raw_s, &bar_raw);
+      pending = blockIdx.x < L.ntiles;
+      int tile_ord = 0;
+      for (int tile = blockIdx.x; tile < L.ntiles; tile += gridDim.x, ++tile_ord) {
+        const int buf = tile_ord % nbuf;
+        const int64_t u0 = (int64_t)tile * 128 * D + L.B0 + L.H;
+        const int64_t base = u0 & ~1LL;
+        bool ok = tc::mbar_wait_bounded(&bar_raw, (uint32_t)(tile_ord & 1), kWaitPolls);
+        if (ok) pending = false;
+        if (ok && tile_ord >= nbuf)
+          ok = tc::mbar_wait_bounded(&bar_in_empty[buf], (uint32_t)((tile_ord / nbuf - 1) & 1), kWaitPolls);
+        if (tc::named_bar_red_or(1, kTcProdThreads, !ok)) {
+          failed = true;
+          break;
+        }
+        uint8_t* A = smem + L.in_off + (size_t)buf * L.in_bytes;
+        int q = tid / V, v = tid - (tid / V) * V;
+        for (int idx = tid; idx < nrec; idx += kTcProdThreads) {
+          const int64_t u = u0 + (v < D ? (int64_t)q * D + v : (int64_t)(q + 1) * D);
+          uint2 x = make_uint2(0u, 0u);
+          if (u >= 0 && u < total) x = raw[u - base];
+          *reinterpret_cast<uint4*>(A + ((size_t)v * Qp + q) * 16) = make_uint4(x.x, x.y, x.x, x.y);
+          v += step_v;
+          q += step_q;
+          if (v >= V) {
+            v -= V;
+            ++q;
+          }
+        }
+        tc::named_bar_sync(1, kTcProdThreads);  // every read of the raw buffer is done
+        const int next = tile + (int)gridDim.x;
+        if (next < L.ntiles) {
+          if (tid == 0) {
+            tc::fence_proxy_async_smem();
+            raw_issue(L, (int64_t)next * 128 * D + L.B0 + L.H, raw_s, &bar_raw);
+          }
+          pending = true;
+        }
+        tc::fence_proxy_async_smem();  // the records are visible to the tensor core
+        __syncwarp();
+        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[buf]);
+      }
+      if (failed) {
+        // a copy still in flight lands before the CTA can exit
+        if (pending) tc::mbar_wait_bounded(&bar_raw, (uint32_t)(tile_ord & 1), kWaitPolls);
+        if (lane_id == 0) atomicExch(L.err, 1);
+      }
+    } else {
     // tiles: record (v, q) of tile t = input sample 128 t D + B0 + q D + v.
     // Up to nbuf - 1 tiles' copies stay in flight; the oldest is announced
     // once its copy group is complete, before the next tile's copies are
@@ -337,6 +430,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         if (lane_id == 0) tc::mbar_arrive(&bar_in_full[announced % nbuf]);
     }
     if (failed && lane_id == 0) atomicExch(L.err, 1);
+    }
   } else if (warp == 3) {
     // ------------------------------------------------------------ MMA issuer
     // A-offset table of every merge set: entry kp = record index (v Qp + q)
@@ -702,7 +796,7 @@ int PolyEngine::groups_idx_of_class(int cls) const {
 // Pre-split [history | block] into packed {hi, lo} pairs (scratch buffer
 // owned by the engine, grown on demand).
 int PolyEngine::prepare_tc_input(const float2* d_in, uint64_t n, cudaStream_t stream) {
-  const size_t need = (size_t)(n + H_);
+  const size_t need = (size_t)(n + H_) + 2;  // one spare pair: bulk copies end on an even sample
   if (need > xhl_cap_) {
     if (d_xhl_) cudaFree(d_xhl_);
     d_xhl_ = nullptr;
@@ -744,7 +838,8 @@ struct TcWsPlan {
 struct TcMsetPlan {
   std::vector<int> ws;   // indices into the work-set list
   int64_t E = 0;         // latest window end
-  int64_t S = 0;         // merged window start (row 0)
+  int64_t S0 = 0;        // earliest window start of its work sets
+  int64_t S = 0;         // merged window start (row 0): E - Kw + 1, Kw rounded up to even
   int Kw = 0;
   int cols = 0;          // 8-column groups x 8
 };
@@ -754,16 +849,17 @@ struct TcLaunchPlan {
   int nws = 0, nslots = 0;
   int64_t B0 = 0;
   int V = 0, Qp = 0, wrap = 0, nbuf = 1;
-  size_t b_bytes = 0, meta_bytes = 0, tab_bytes = 0, in_bytes = 0;
+  int raw_span = 0;      // > 0: tiles staged through one bulk copy of their input span
+  size_t b_bytes = 0, meta_bytes = 0, tab_bytes = 0, in_bytes = 0, raw_bytes = 0;
 };
 
-// [B of each merge set | slot constants | A-offset tables | input buffers]
+// [B of each merge set | slot constants | A-offset tables | raw span | input buffers]
 size_t tc_smem_need(const TcLaunchPlan& p, int nbuf) {
-  return ((p.b_bytes + p.meta_bytes + p.tab_bytes + 127) & ~(size_t)127) + (size_t)nbuf * p.in_bytes;
+  return ((p.b_bytes + p.meta_bytes + p.tab_bytes + 127) & ~(size_t)127) + p.raw_bytes + (size_t)nbuf * p.in_bytes;
 }
 
 // Staging geometry of a launch covering merge sets p.ms.
-void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t D) {
+void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t D, bool allow_raw = true) {
   p.B0 = INT64_MAX;
   p.b_bytes = p.meta_bytes = p.tab_bytes = 0;
   p.nws = p.nslots = 0;
@@ -781,6 +877,21 @@ void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t
   p.wrap = W > (int64_t)D ? 1 : 0;
   p.V = p.wrap ? (int)D + 1 : (int)W;
   p.Qp = p.wrap ? 128 + (int)((W - 1) / D) : 128;
+  // wrapped windows read (nearly) every sample of the tile's span: stage
+  // them with one bulk copy when the span is small enough (Qp odd keeps the
+  // record writes free of bank conflicts)
+  p.raw_span = 0;
+  p.raw_bytes = 0;
+  if (p.wrap && allow_raw) {
+    const int qp = p.Qp | 1;
+    const size_t span = (size_t)qp * D + 1;
+    const size_t bytes = (((span + 2) * 8) + 127) & ~(size_t)127;
+    if (bytes <= kTcRawMax) {
+      p.Qp = qp;
+      p.raw_span = (int)span;
+      p.raw_bytes = bytes;
+    }
+  }
   p.in_bytes = (((size_t)p.V * p.Qp * 16) + 127) & ~(size_t)127;
 }
 
@@ -791,16 +902,17 @@ std::vector<TcMsetPlan> tc_merge(const std::vector<TcWsPlan>& wl, const std::vec
   for (int wi : order) {
     const TcWsPlan& w = wl[wi];
     const int64_t s = w.delta - w.ch->T + 1;
-    const int cols = 8 * w.ch->ng;
+    const int cols = 2 * (int)w.ch->chans.size();
     bool joined = false;
     if (!msets.empty()) {
       TcMsetPlan& m = msets.back();
       const int64_t E = std::max(m.E, w.delta);
-      const int64_t S = std::min(m.S, s);
-      const int Kw = (int)(((E - S + 1) + 1) & ~1LL);
+      const int64_t S0 = std::min(m.S0, s);
+      const int Kw = (int)(((E - S0 + 1) + 1) & ~1LL);
       if (m.cols + cols <= cap && Kw <= kTcMaxKw) {
         m.ws.push_back(wi);
         m.E = E;
+        m.S0 = S0;
         m.S = E - Kw + 1;
         m.Kw = Kw;
         m.cols += cols;
@@ -812,6 +924,7 @@ std::vector<TcMsetPlan> tc_merge(const std::vector<TcWsPlan>& wl, const std::vec
       m.ws.push_back(wi);
       m.E = w.delta;
       m.Kw = w.ch->T;
+      m.S0 = s;
       m.S = m.E - m.Kw + 1;
       m.cols = cols;
       msets.push_back(m);
@@ -830,6 +943,7 @@ bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, std::vector<TcLau
       TcLaunchPlan p = plans.back();
       p.ms.push_back(mi);
       tc_geometry(msets, p, D);
+      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, false);
       if (tc_smem_need(p, 1) <= kTcSmemMax && p.nws <= kMaxTcWorkSets && p.nslots <= kMaxTcSlots) {
         plans.back() = p;
         joined = true;
@@ -839,6 +953,7 @@ bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, std::vector<TcLau
       TcLaunchPlan p;
       p.ms.push_back(mi);
       tc_geometry(msets, p, D);
+      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, false);
       if (tc_smem_need(p, 1) > kTcSmemMax || p.nws > kMaxTcWorkSets || p.nslots > kMaxTcSlots) return false;
       plans.push_back(p);
     }
@@ -925,7 +1040,7 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
       M.boff = (int32_t)off;
       off += (size_t)M.N * M.Kw * 16;
       M.ws_begin = nws;
-      int cg = 0;
+      int s0 = 0;
       for (int wi : m.ws) {
         const TcWsPlan& w = wl[wi];
         TcWorkSet& W = L.ws[nws++];
@@ -940,8 +1055,8 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
         W.U = (int32_t)w.U;
         W.r = (int32_t)w.r;
         W.o = (int32_t)((w.delta - w.ch->T + 1) - m.S);
-        W.cg0 = cg;
-        cg += w.ch->ng;
+        W.s0 = s0;
+        s0 += W.n;
         rows = std::max(rows, w.J);
       }
       M.ws_end = nws;
@@ -957,9 +1072,9 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
         h.invR = 1.0f / (float)h.R;
         for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
           const TcWorkSet& W = L.ws[wi];
-          const int i = sI - 4 * W.cg0;
-          if (i < 0 || i >= 4 * W.ng) continue;
-          if (i < W.n) {
+          const int i = sI - W.s0;
+          if (i < 0 || i >= W.n) continue;
+          {
             const TcWsPlan& w = wl[msets[p.ms[q]].ws[wi - M.ws_begin]];
             const int c = w.ch->chans[i];
             const NcoConst& nc = chans_[c].nco;
@@ -990,6 +1105,9 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
     }
     off += (size_t)toff * 4;
     off = (off + 127) & ~(size_t)127;
+    L.raw_off = (int32_t)off;
+    L.raw_span = p.raw_span;
+    off += p.raw_bytes;
     L.in_off = (int32_t)off;
     L.in_bytes = (int32_t)p.in_bytes;
     L.nbuf = p.nbuf;

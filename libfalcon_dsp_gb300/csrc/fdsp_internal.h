@@ -114,7 +114,7 @@ struct TcWorkSet {
   int32_t U;             // class up rate (output m = r + U j)
   int32_t r;
   int32_t o;             // tap offset of its window inside the merge set's window
-  int32_t cg0;           // first 8-column group inside the merge set's B
+  int32_t s0;            // first slot (column pair) inside the merge set's B
   int32_t pad_;
 };
 
@@ -167,6 +167,8 @@ struct TcLaunch {
   int32_t in_bytes;                  // bytes of one input buffer
   int32_t nbuf;                      // input buffers (1 to 4)
   int32_t tab_off;                   // shared-memory byte offset of the A-offset tables
+  int32_t raw_off;                   // shared-memory byte offset of the raw span buffer
+  int32_t raw_span;                  // samples of a tile's raw span (0: per-record staging)
   TcMset ms[kMaxTcMsets];
   TcSlotHot slot[kMaxTcSlots];
   TcWorkSet ws[kMaxTcWorkSets];
