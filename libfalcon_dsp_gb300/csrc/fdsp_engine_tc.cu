@@ -279,11 +279,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
               sm.nco.rollover = nc.rollover;
               sm.nco.base = L.nco_base[c];
               sm.nco.enabled = nc.enabled;
-              // fast path: R < 2^31 (row counters in 32 bits); the counter
-              // of row `row` is row 0's plus row D, past the rollover at most
-              // once when 127 D + T < R, else reduced with the fast modulo;
-              // R >= 2^31 ("general") takes the exact path for every output
-              const bool general = nc.enabled && nc.rollover >= 0x80000000u;
+              // fast path: R < 2^31 (row counters in 32 bits) and
+              // 127 D + T < R, so the counter of row `row` is row 0's plus
+              // row D, past the rollover at most once (R >= 1e5 by
+              // construction, so this holds for D up to ~780); otherwise
+              // ("general") every output takes the exact path
+              const bool general =
+                  nc.enabled && (nc.rollover >= 0x80000000u || 127LL * D + W.T >= (int64_t)nc.rollover);
               sm.fastmod = nc.fastmod;
               sm.om_lo = nc.enabled && !general ? (uint32_t)nc.omega64 : 0u;
               sm.om_hi = nc.enabled && !general ? (uint32_t)(nc.omega64 >> 32) : 0u;
@@ -303,6 +305,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
           }
         }
         reinterpret_cast<SlotMeta*>(smem + M.moff)[s] = sm;
+        // the row-0 counter inputs again, one array per field (lanes of the
+        // epilogue read consecutive slots without bank conflicts): window
+        // start of row 0 in samples since reset, R, the fast-modulo constant,
+        // and whether the slot rotates on the fast path
+        uint32_t* P0in = reinterpret_cast<uint32_t*>(smem + M.poff);
+        const int NS = M.N >> 1;
+        const int64_t x0 = (int64_t)sm.nco.base + sm.delta - sm.T + 1;
+        P0in[s] = (uint32_t)(uint64_t)x0;
+        P0in[NS + s] = (uint32_t)((uint64_t)x0 >> 32);
+        P0in[2 * NS + s] = sm.R;
+        P0in[3 * NS + s] = (uint32_t)sm.fastmod;
+        P0in[4 * NS + s] = (uint32_t)(sm.fastmod >> 32);
+        P0in[5 * NS + s] = (sm.om_lo | sm.om_hi) ? 1u : 0u;
       }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -543,6 +558,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       tc::fence_after_sync();
       const TcMset& M = L.ms[mi];
       const SlotMeta* meta = reinterpret_cast<const SlotMeta*>(smem + M.moff);
+      const uint32_t* P0in = reinterpret_cast<const uint32_t*>(smem + M.poff);
       const int nslots = M.N >> 1;
       const int64_t j0 = (int64_t)tile * 128;
       const int64_t j = j0 + row;
@@ -554,15 +570,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int si = lane_id + 32 * h;
-        if (si < nslots) {
-          const SlotMeta& sm = meta[si];
-          if (sm.om_lo | sm.om_hi) {
-            // x < R + 2^31 < 2^32 on the fast path; x >= -(T - 1) > -R
-            const int64_t x = (int64_t)sm.nco.base + sm.delta - sm.T + 1 + j0 * D;
-            const uint32_t pr0 = x < 0 ? (uint32_t)(x + sm.R)
-                                       : (uint32_t)__umul64hi(sm.nco.fastmod * (uint64_t)x, (uint64_t)sm.R);
-            if (h == 0) p0a = pr0; else p0b = pr0;
-          }
+        if (si < nslots && P0in[5 * nslots + si]) {
+          // x < R + 2^31 < 2^32 on the fast path; x >= -(T - 1) > -R
+          const int64_t x0 = (int64_t)(((uint64_t)P0in[nslots + si] << 32) | P0in[si]);
+          const int64_t x = x0 + j0 * D;
+          const uint32_t R = P0in[2 * nslots + si];
+          const uint64_t fm = ((uint64_t)P0in[4 * nslots + si] << 32) | P0in[3 * nslots + si];
+          const uint32_t pr0 = x < 0 ? (uint32_t)(x + R) : (uint32_t)__umul64hi(fm * (uint64_t)x, (uint64_t)R);
+          if (h == 0) p0a = pr0; else p0b = pr0;
         }
       }
       const uint32_t rowD = (uint32_t)(row * D);
@@ -592,15 +607,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
           const TcSlotHot sh = hot[e];
           const uint32_t P0 = __shfl_sync(0xffffffffu, si < 32 ? p0a : p0b, si & 31);
           const uint32_t R = sh.R;
-          // (P0 + row D) mod R without a branch: quotient estimate from 1/R
-          // in FP32 (off by at most one for these magnitudes), then one
-          // correction each way
+          // (P0 + row D) mod R: P0 < R and row D < R - T on the fast path,
+          // so one conditional subtraction
           const uint32_t a = P0 + rowD;
-          const uint32_t qe = __float2uint_rz(__uint2float_rz(a) * sh.invR);
-          int64_t rem = (int64_t)a - (int64_t)qe * R;  // in [-R, 2R)
-          rem = rem < 0 ? rem + R : rem;
-          rem = rem >= (int64_t)R ? rem - R : rem;
-          const uint32_t pc = (uint32_t)rem;
+          const uint32_t pc = a >= R ? a - R : a;
           const bool okr = pc + sh.Tm1 < R;
           // bits 32..63 of pc * omega64: the phase in 2^-32 turns
           const uint32_t turns = __umulhi(pc, sh.om_lo) + pc * sh.om_hi;
@@ -869,7 +879,7 @@ void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t
     p.nws += (int)msets[m].ws.size();
     p.nslots += N / 2;
     p.b_bytes += (size_t)N * msets[m].Kw * 16;
-    p.meta_bytes += (size_t)(N / 2) * sizeof(SlotMeta);
+    p.meta_bytes += (size_t)(N / 2) * (sizeof(SlotMeta) + 6 * sizeof(uint32_t));
     p.tab_bytes += (size_t)((msets[m].Kw / 2 + 3) & ~3) * 4;
   }
   int64_t W = 0;
@@ -1069,7 +1079,6 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
       for (int sI = 0; sI < M.N / 2; ++sI) {
         TcSlotHot& h = L.slot[nslot++];
         h.R = 0x7fffffffu;
-        h.invR = 1.0f / (float)h.R;
         for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
           const TcWorkSet& W = L.ws[wi];
           const int i = sI - W.s0;
@@ -1078,7 +1087,8 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
             const TcWsPlan& w = wl[msets[p.ms[q]].ws[wi - M.ws_begin]];
             const int c = w.ch->chans[i];
             const NcoConst& nc = chans_[c].nco;
-            const bool general = nc.enabled && nc.rollover >= 0x80000000u;
+            const bool general =
+                nc.enabled && (nc.rollover >= 0x80000000u || 127LL * D + W.T >= (int64_t)nc.rollover);
             h.om_lo = nc.enabled && !general ? (uint32_t)nc.omega64 : 0u;
             h.om_hi = nc.enabled && !general ? (uint32_t)(nc.omega64 >> 32) : 0u;
             h.out_lo = (uint32_t)(uintptr_t)out[c];
@@ -1087,7 +1097,6 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
             h.Tm1 = general ? 0x7fffffffu : (uint32_t)(W.T - 1);
             h.ur = (uint32_t)W.U | ((uint32_t)W.r << 16);
             h.J = W.J;
-            h.invR = 1.0f / (float)h.R;
           }
           break;
         }
@@ -1096,6 +1105,8 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
     for (size_t q = 0; q < p.ms.size(); ++q) {
       L.ms[q].moff = (int32_t)off;
       off += (size_t)(L.ms[q].N / 2) * sizeof(SlotMeta);
+      L.ms[q].poff = (int32_t)off;
+      off += (size_t)(L.ms[q].N / 2) * 6 * sizeof(uint32_t);
     }
     L.tab_off = (int32_t)off;
     int toff = 0;

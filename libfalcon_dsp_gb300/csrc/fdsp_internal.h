@@ -130,7 +130,8 @@ struct TcMset {
   int32_t ws_begin, ws_end;
   int32_t toff;          // first entry of its A-offset table (multiple of 4)
   int32_t slot0;         // first entry of its channel slots in TcLaunch::slot
-  int32_t pad_[3];
+  int32_t poff;          // shared-memory byte offset of its row-0 counter inputs (one array per field)
+  int32_t pad_[2];
 };
 
 // Per-output constants of one channel slot, read by every output of the
@@ -143,8 +144,6 @@ struct TcSlotHot {
   uint32_t Tm1;           // taps - 1 (0x7fffffff: every output on the exact path)
   uint32_t ur;            // U | r << 16 (output m = r + U j)
   int32_t J;              // rows with an output (0: padding slot)
-  float invR;             // 1 / R (row counter reduction)
-  uint32_t pad_[3];
 };
 
 struct TcLaunch {
