@@ -55,7 +55,7 @@
 
 namespace fdsp {
 
-constexpr int kTcThreads = 640;       // 3 producer warps + 1 MMA warp + 16 epilogue warps
+constexpr int kTcThreads = 672;       // 3 producer warps + 2 MMA warps (3, 20) + 16 epilogue warps
 constexpr int kTcProdThreads = 96;    // (20 warps: 5 per SM sub-partition, up to 96 registers each)
 constexpr int kTcDSlots = 4;          // accumulator slots = epilogue groups (items in flight)
 constexpr uint32_t kTcDCols = 128;    // accumulator columns per slot (N <= 128)
@@ -154,6 +154,31 @@ __device__ __forceinline__ void stage_half(const TcLaunch& L, int64_t v, uint32_
     bytes = 8;
   }
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+
+// Tile schedule shared by every role.  With two or more input buffers two
+// MMA warps issue alternate tiles (one issuing thread does not keep the
+// tensor pipe busy with MMAs this narrow): tile t goes to warp w = t % 2 as
+// its (t / 2)-th tile, and warp w owns input buffers [w nbw, (w + 1) nbw)
+// and accumulator slots {2w, 2w + 1}.  Every barrier then has one waiter,
+// which consumes its phases in order (parity waits never alias).
+struct TcSched {
+  int nw;   // MMA warps in use (1 or 2)
+  int nbw;  // input buffers per MMA warp
+  int spw;  // accumulator slots per MMA warp
+};
+__device__ __forceinline__ TcSched tc_sched(int nbuf) {
+  TcSched s;
+  s.nw = nbuf >= 2 ? 2 : 1;
+  s.nbw = nbuf / s.nw;
+  s.spw = kTcDSlots / s.nw;
+  return s;
+}
+// input buffer of tile t and how many earlier tiles used it
+__device__ __forceinline__ int tc_buf(const TcSched& s, int t, int* use) {
+  const int w = t % s.nw, k = t / s.nw;
+  *use = k / s.nbw;
+  return w * s.nbw + k % s.nbw;
 }
 
 // Bulk copy (one TMA transfer) of the {hi, lo} pairs of absolute samples
@@ -336,7 +361,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       const uint32_t raw_s = tc::smem_u32(smem + L.raw_off);
       const uint2* raw = reinterpret_cast<const uint2*>(smem + L.raw_off);
       const int64_t total = L.N + L.H;
-      const int V = L.V, Qp = L.Qp, nbuf = L.nbuf;
+      const int V = L.V, Qp = L.Qp;
+      const TcSched S = tc_sched(L.nbuf);
       const int nrec = V * Qp;
       const int step_q = kTcProdThreads / V, step_v = kTcProdThreads % V;
       bool pending = false;
@@ -344,13 +370,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       pending = blockIdx.x < L.ntiles;
       int tile_ord = 0;
       for (int tile = blockIdx.x; tile < L.ntiles; tile += gridDim.x, ++tile_ord) {
-        const int buf = tile_ord % nbuf;
+        int use = 0;
+        const int buf = tc_buf(S, tile_ord, &use);
         const int64_t u0 = (int64_t)tile * 128 * D + L.B0 + L.H;
         const int64_t base = u0 & ~1LL;
         bool ok = tc::mbar_wait_bounded(&bar_raw, (uint32_t)(tile_ord & 1), kWaitPolls);
         if (ok) pending = false;
-        if (ok && tile_ord >= nbuf)
-          ok = tc::mbar_wait_bounded(&bar_in_empty[buf], (uint32_t)((tile_ord / nbuf - 1) & 1), kWaitPolls);
+        if (ok && use >= 1) ok = tc::mbar_wait_bounded(&bar_in_empty[buf], (uint32_t)((use - 1) & 1), kWaitPolls);
         if (tc::named_bar_red_or(1, kTcProdThreads, !ok)) {
           failed = true;
           break;
@@ -393,8 +419,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     // once its copy group is complete, before the next tile's copies are
     // issued (the buffer of tile t is reused for tile t + nbuf after the
     // MMAs of tile t are done).
-    const int nbuf = L.nbuf;
-    const int lag = nbuf - 1;
+    const TcSched S = tc_sched(L.nbuf);
+    const int lag = S.nw * S.nbw - 1;  // buffers in use - 1
     int tile_ord = 0;
     int announced = 0;
     // staging map: lanes 2i, 2i+1 write the two halves of record (v, q),
@@ -403,7 +429,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     const uint32_t half = (uint32_t)(tid & 1) * 8u;
     const int rsub = tid >> 1;  // 0..47
     for (int tile = blockIdx.x; tile < L.ntiles; tile += gridDim.x, ++tile_ord) {
-      const int buf = tile_ord % nbuf;
+      int use = 0;
+      const int buf = tc_buf(S, tile_ord, &use);
       if (tile_ord >= lag && lag > 0) {
         switch (lag) {  // all but the lag - 1 most recent groups
           case 1: asm volatile("cp.async.wait_group 0;\n" ::: "memory"); break;
@@ -412,12 +439,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         }
         tc::fence_proxy_async_smem();
         __syncwarp();
-        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[announced % nbuf]);
+        int ua = 0;
+        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[tc_buf(S, announced, &ua)]);
         ++announced;
       }
-      if (tile_ord >= nbuf) {
-        const int use = tile_ord / nbuf - 1;  // earlier use of this buffer
-        const bool ok = tc::mbar_wait_bounded(&bar_in_empty[buf], (uint32_t)(use & 1), kWaitPolls);
+      if (use >= 1) {  // the buffer's previous tile has been consumed
+        const bool ok = tc::mbar_wait_bounded(&bar_in_empty[buf], (uint32_t)((use - 1) & 1), kWaitPolls);
         if (__any_sync(0xffffffffu, !ok)) {
           failed = true;
           break;
@@ -433,7 +460,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         tc::fence_proxy_async_smem();
         __syncwarp();
-        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[0]);
+        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[buf]);
         ++announced;
       }
     }
@@ -441,18 +468,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     if (!failed) {
       tc::fence_proxy_async_smem();
       __syncwarp();
-      for (; announced < tile_ord; ++announced)
-        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[announced % nbuf]);
+      for (; announced < tile_ord; ++announced) {
+        int ua = 0;
+        if (lane_id == 0) tc::mbar_arrive(&bar_in_full[tc_buf(S, announced, &ua)]);
+      }
     }
     if (failed && lane_id == 0) atomicExch(L.err, 1);
     }
-  } else if (warp == 3) {
+  } else if (warp == 3 || warp == kTcThreads / 32 - 1) {
     // ------------------------------------------------------------ MMA issuer
     // A-offset table of every merge set: entry kp = record index (v Qp + q)
     // of taps 2kp, 2kp+1 in a staged tile, i.e. the A descriptor's address
     // field relative to the buffer (computed once, by all 32 lanes)
+    const TcSched S = tc_sched(L.nbuf);
+    const int mw = warp == 3 ? 0 : 1;
     uint32_t* tab = reinterpret_cast<uint32_t*>(smem + L.tab_off);
-    for (int mi = 0; mi < nms; ++mi) {
+    for (int mi = 0; mi < nms && mw == 0; ++mi) {
       const TcMset& M = L.ms[mi];
       const int nkp = M.Kw / 2;
       for (int kp = lane_id; kp < ((nkp + 3) & ~3); kp += 32) {
@@ -465,18 +496,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         tab[M.toff + kp] = e;
       }
     }
-    __syncwarp();
+    tc::named_bar_sync(2, 64);  // both MMA warps: the table is written before it is read
     bool ok = tc::mbar_wait_bounded(&bar_b_full, 0u, kWaitPolls);
     if (__any_sync(0xffffffffu, !ok)) failed = true;
-    int it = 0;
-    int tile_ord = 0;
-    const int nbuf = L.nbuf;
+    if (mw >= S.nw) failed = true;  // second MMA warp unused: one input buffer
     // descriptor words: low = address >> 4 | (leading byte offset >> 4) << 16,
     // high = (stride byte offset >> 4) | version 1 (bit 46)
     const uint32_t a_hi = (128u >> 4) | (1u << 14);
-    for (int tile = blockIdx.x; !failed && tile < L.ntiles; tile += gridDim.x, ++tile_ord) {
-      const int buf = tile_ord % nbuf;
-      const int use = tile_ord / nbuf;
+    int tile_ord = mw;
+    for (int tile = blockIdx.x + mw * (int)gridDim.x; !failed && tile < L.ntiles;
+         tile += S.nw * (int)gridDim.x, tile_ord += S.nw) {
+      int use = 0;
+      const int buf = tc_buf(S, tile_ord, &use);
       ok = tc::mbar_wait_bounded(&bar_in_full[buf], (uint32_t)(use & 1), kWaitPolls);
       if (__any_sync(0xffffffffu, !ok)) {
         failed = true;
@@ -485,10 +516,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       tc::fence_after_sync();
       const uint32_t xb = tc::smem_u32(smem + L.in_off + buf * L.in_bytes);
       const uint32_t a_lo0 = ((xb >> 4) & 0x3FFFu) | ((((uint32_t)L.Qp * 16u) >> 4) << 16);
-      for (int mi = 0; mi < nms; ++mi, ++it) {
-        const uint32_t ds = (uint32_t)(it % kTcDSlots);
-        if (it >= kTcDSlots) {
-          ok = tc::mbar_wait_bounded(&bar_d_empty[ds], (uint32_t)(((it - kTcDSlots) / kTcDSlots) & 1), kWaitPolls);
+      for (int mi = 0; mi < nms; ++mi) {
+        const int jw = (tile_ord / S.nw) * nms + mi;  // this warp's item number
+        const uint32_t ds = (uint32_t)(mw * S.spw + jw % S.spw);
+        const int suse = jw / S.spw;
+        if (suse >= 1) {
+          ok = tc::mbar_wait_bounded(&bar_d_empty[ds], (uint32_t)((suse - 1) & 1), kWaitPolls);
           if (__any_sync(0xffffffffu, !ok)) {
             failed = true;
             break;
@@ -532,7 +565,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       if (lane_id == 0) tc::mma_commit(&bar_in_empty[buf]);
       __syncwarp();
     }
-    if (failed && lane_id == 0) atomicExch(L.err, 1);
+    if (failed && mw < S.nw && lane_id == 0) atomicExch(L.err, 1);
   } else {
     // ------------------------------------------------------------ epilogue
     // Group eg drains items eg, eg+4, ... (item = tile_ord * nmsets + merge
@@ -545,12 +578,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     const int row = quarter * 32 + lane_id;
     bool ok = tc::mbar_wait_bounded(&bar_b_full, 0u, kWaitPolls);
     if (__any_sync(0xffffffffu, !ok)) failed = true;
-    for (int it = eg; !failed; it += kTcDSlots) {
-      const int tile_ord = it / nms;
-      const int mi = it - tile_ord * nms;
+    // slot eg belongs to MMA warp eg / spw; its items are that warp's items
+    // eg % spw, eg % spw + spw, ...
+    const TcSched S = tc_sched(L.nbuf);
+    const int ew = eg / S.spw;
+    for (int jw = eg % S.spw; !failed; jw += S.spw) {
+      const int kt = jw / nms;
+      const int mi = jw - kt * nms;
+      const int tile_ord = kt * S.nw + ew;
       const int tile = blockIdx.x + tile_ord * gridDim.x;
       if (tile >= L.ntiles) break;
-      ok = tc::mbar_wait_bounded(&bar_d_full[eg], (uint32_t)((it / kTcDSlots) & 1), kWaitPolls);
+      ok = tc::mbar_wait_bounded(&bar_d_full[eg], (uint32_t)((jw / S.spw) & 1), kWaitPolls);
       if (__any_sync(0xffffffffu, !ok)) {
         failed = true;
         break;
