@@ -175,10 +175,116 @@ __device__ __forceinline__ void process_row(const float2* __restrict__ xs, const
   }
 }
 
+// Single-channel work sets with long filters: each thread computes kWinRows
+// consecutive output rows.  Taps are visited phase by phase (k = v, v + D,
+// ...), where the samples of consecutive taps and consecutive rows are
+// consecutive in the de-interleaved tile, so the rows share one sliding
+// window of samples held in registers: one shared-memory load per tap step
+// serves kWinRows outputs (the per-row path loads a sample per tap and
+// output).  kWinRows is odd so the lanes of a warp (row blocks kWinRows
+// apart) read distinct bank pairs.  Real taps (no NCO shift, resampler
+// semantics) take 2 FMAs per tap instead of 4.
+constexpr int kWinRows = 7;
+
+template <bool kReal>
+__device__ __forceinline__ void win_mac(float2& acc, float2 g, float2 x) {
+  if constexpr (kReal) {
+    acc.x = fmaf(g.x, x.x, acc.x);
+    acc.y = fmaf(g.x, x.y, acc.y);
+  } else {
+    acc.x = fmaf(g.x, x.x, acc.x);
+    acc.x = fmaf(-g.y, x.y, acc.x);
+    acc.y = fmaf(g.x, x.y, acc.y);
+    acc.y = fmaf(g.y, x.x, acc.y);
+  }
+}
+
+// Rotation and store of one single-channel output (the per-row epilogue
+// for NB = 1, taps at stride 2 float2).
+__device__ __forceinline__ void win_finish(float2 acc, const ChanMeta& cm, const float2* __restrict__ xs,
+                                           const float2* __restrict__ tp, int T, int D, int P, int a0, int jl,
+                                           int64_t j, int U, int r, int delta) {
+  const int64_t m = (int64_t)r + (int64_t)U * j;
+  const int64_t w = (int64_t)delta + j * D - T + 1;
+  float2 y = acc;
+  if (rotate_fast(cm, w, T, y)) {
+    cm.out[m] = y;
+    return;
+  }
+  const ExactRot er = rotate_prep(cm, w, T);
+  float2 B = make_float2(0.f, 0.f);
+  if (er.straddle) {
+    const int kb = a0 + er.k0;
+    int qq = kb / D;
+    int bb = kb - qq * D;
+    qq += jl;
+    for (int k = er.k0; k < T; ++k) {
+      const float2 x = xs[bb * P + qq];
+      const float2 gk = tp[k * 2];
+      B.x = fmaf(gk.x, x.x, B.x);
+      B.x = fmaf(-gk.y, x.y, B.x);
+      B.y = fmaf(gk.x, x.y, B.y);
+      B.y = fmaf(gk.y, x.x, B.y);
+      if (++bb == D) {
+        bb = 0;
+        ++qq;
+      }
+    }
+  }
+  cm.out[m] = rotate_apply(er, acc, B);
+}
+
+template <bool kReal>
+__device__ __forceinline__ void process_rows_win(const float2* __restrict__ xs, const float2* __restrict__ tp,
+                                                 const ChanMeta* __restrict__ meta, int T, int D, int P, int a0,
+                                                 int jl0, int64_t j0, int64_t J, int U, int r, int delta) {
+  float2 acc[kWinRows];
+#pragma unroll
+  for (int q = 0; q < kWinRows; ++q) acc[q] = make_float2(0.f, 0.f);
+  const int bq = a0 / D, b0 = a0 - bq * D;
+  const int nv = T < D ? T : D;
+  for (int vp = 0; vp < nv; ++vp) {
+    int ph = b0 + vp, q0 = bq + jl0;
+    if (ph >= D) {
+      ph -= D;
+      ++q0;
+    }
+    const float2* xr = xs + ph * P + q0;  // row jl0 + q, tap vp + m D: xr[m + q]
+    const float2* tk = tp + 2 * vp;       // tap k at tp[2 k]
+    const int tstep = 2 * D;
+    const int nm = (T - 1 - vp) / D + 1;
+    float2 w[kWinRows];
+#pragma unroll
+    for (int q = 0; q < kWinRows - 1; ++q) w[q] = xr[q];
+    int m = 0;
+    for (; m + kWinRows <= nm; m += kWinRows) {
+      // circular window: sample m + u + q sits in slot (u + q) % kWinRows
+#pragma unroll
+      for (int u = 0; u < kWinRows; ++u) {
+        w[(u + kWinRows - 1) % kWinRows] = xr[m + u + kWinRows - 1];
+        const float2 g = tk[(m + u) * tstep];
+#pragma unroll
+        for (int q = 0; q < kWinRows; ++q) win_mac<kReal>(acc[q], g, w[(u + q) % kWinRows]);
+      }
+    }
+    for (; m < nm; ++m) {
+      w[kWinRows - 1] = xr[m + kWinRows - 1];
+      const float2 g = tk[m * tstep];
+#pragma unroll
+      for (int q = 0; q < kWinRows; ++q) win_mac<kReal>(acc[q], g, w[q]);
+#pragma unroll
+      for (int q = 0; q < kWinRows - 1; ++q) w[q] = w[q + 1];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kWinRows; ++q)
+    if (j0 + q < J) win_finish(acc[q], meta[0], xs, tp, T, D, P, a0, jl0 + q, j0 + q, U, r, delta);
+}
+
 // One CTA = one tile of Qt output rows of decimation group g.  Shared memory:
 // [input tile, de-interleaved: D x P float2][taps of every work set of the
 // group, packed [T][nb]][ChanMeta per (work set, channel)].
-template <int NBMAX, bool kTapsSmem>
+template <int NBMAX, bool kTapsSmem, bool kWin>
 __global__ void __launch_bounds__(kThreads, 3) poly_fp32_kernel(const __grid_constant__ PolyLaunch<NBMAX> L, int g) {
   extern __shared__ __align__(16) float2 xs[];
   // g < 0: one launch over several groups (small blocks), group =
@@ -260,6 +366,29 @@ __global__ void __launch_bounds__(kThreads, 3) poly_fp32_kernel(const __grid_con
   }
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
+
+  if constexpr (kWin) {
+    // single-channel work sets: items are (work set, block of kWinRows rows),
+    // blocks fastest (Qt is a multiple of 32 kWinRows)
+    const int nblk = Qt / kWinRows;
+    const int nitems = nws * nblk;
+    for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+      const int wq = it / nblk;
+      const int jl0 = (it - wq * nblk) * kWinRows;
+      const WorkSet<NBMAX>& W = L.ws[G.ws_begin + wq];
+      const int64_t j0 = row0 + jl0;
+      if (j0 >= W.J) continue;
+      const int T = W.T;
+      const int a0 = (W.delta - G.delta_min) + (G.tmax - T);
+      const float2* tp = kTapsSmem ? taps_s + W.soff : W.taps;
+      const ChanMeta* mt = meta_s + wq * NBMAX;
+      if (G.real_taps)
+        process_rows_win<true>(xs, tp, mt, T, D, P, a0, jl0, j0, W.J, W.U, W.r, W.delta);
+      else
+        process_rows_win<false>(xs, tp, mt, T, D, P, a0, jl0, j0, W.J, W.U, W.r, W.delta);
+    }
+    return;
+  }
 
   // Items are (work set, row) with rows fastest; Qt is a multiple of 32 so a
   // warp never mixes work sets and every tap load is a broadcast.
@@ -446,6 +575,37 @@ int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool
     g.Qt = choose_qt(g.D, tmax);
     if (g.Qt < 0) return FDSP_ERR_UNSUPPORTED;
     g.Qt_default = g.Qt;
+    // sliding-window form: every batch of the group holds one channel and
+    // the filter is long enough for row blocks to pay; tiles of a multiple
+    // of 32 x kWinRows rows within the same shared-memory budget
+    bool single = true, real = true;
+    for (int b : g.batches) {
+      single = single && batches_[b].chans.size() == 1;
+      for (int c : batches_[b].chans) {
+        real = real && !chans_[c].nco.enabled;
+        for (const float2& h : chans_[c].flipped) real = real && h.y == 0.f;
+      }
+    }
+    const int unit = 32 * kWinRows;
+    if (single && tmax >= 16) {
+      auto bytes = [&](int q) {
+        const int64_t len = (int64_t)q * g.D + 3LL * g.D + tmax;
+        return (int64_t)g.D * (len / g.D + 2) * 8;
+      };
+      // enough row blocks for every thread of the CTA: kThreads blocks of
+      // kWinRows rows spread over the group's work sets (U output phases each
+      // class), as far as shared memory allows
+      size_t nws = 0;
+      for (int b : g.batches) nws += classes_[batches_[b].cls].up;
+      const int want = (int)((kThreads + std::max<size_t>(nws, 1) - 1) / std::max<size_t>(nws, 1)) * kWinRows;
+      int q = std::max(unit, (want + unit - 1) / unit * unit);
+      while (q > unit && bytes(q) > 200 * 1024) q -= unit;
+      if (bytes(q) <= 200 * 1024) {
+        g.win = 1;
+        g.real_taps = real ? 1 : 0;
+        g.Qt_win = q;
+      }
+    }
   }
 
   // modulated, padded taps of every batch: [up][T][NB]
@@ -653,6 +813,12 @@ template <int NB>
 int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream) {
   static thread_local PolyLaunch<NB> L;  // ~20 KB: keep it off the stack
   std::memset(&L, 0, sizeof(L));
+  if (num_sms_ == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev);
+    if (num_sms_ <= 0) num_sms_ = 1;
+  }
   L.block = in16_ ? nullptr : d_in;
   L.block16 = in16_;
   L.hist = d_hist_[hist_cur_];
@@ -669,7 +835,6 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
   for (auto& g : groups_) {
     GroupDesc& gd = L.groups[ng];
     gd.D = (int32_t)g.D;
-    gd.Qt = g.Qt;
     gd.ws_begin = nws;
     int dmin = INT32_MAX, dmax = INT32_MIN, tmax = 1;
     int64_t rows = 0;
@@ -704,8 +869,15 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
     gd.tmax = tmax;
     gd.delta_min = dmin;
     gd.delta_span = dmax - dmin;
-    gd.ntiles = (int32_t)((rows + g.Qt - 1) / g.Qt);
-    const int64_t len = (int64_t)g.Qt * g.D + gd.delta_span + tmax - 1;
+    // the sliding-window form where it fills the GPU with its larger tiles
+    // (short blocks keep the per-row form, whose smaller tiles spread wider)
+    const bool win = g.win && rows >= (int64_t)g.Qt_win * num_sms_;
+    const int Qt = win ? g.Qt_win : g.Qt;
+    gd.Qt = Qt;
+    gd.win = win ? 1 : 0;
+    gd.real_taps = g.real_taps;
+    gd.ntiles = (int32_t)((rows + Qt - 1) / Qt);
+    const int64_t len = (int64_t)Qt * g.D + gd.delta_span + tmax - 1;
     int64_t P = (len + g.D - 1) / g.D;
     if ((P & 1) == 0) P++;  // odd pitch: the staging scatter spreads over banks
     gd.P = (int32_t)P;
@@ -760,19 +932,21 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
     }
     if (fuse && tiles <= 3LL * num_sms_ && L.max_tiles > 0) {
       int nm = 0;
-      for (int pass = 0; pass < 2; ++pass) {
+      for (int pass = 0; pass < 4; ++pass) {  // (taps in shared memory?, sliding window?)
         const int first = nm;
         size_t fsmem = 0;
         int ftiles = 0;
+        const int want_smem = (pass & 1) == 0 ? 1 : 0, want_win = pass >> 1;
         for (int gi = 0; gi < ng; ++gi) {
           const GroupDesc& gd = L.groups[gi];
-          if (gd.taps_smem != (pass == 0 ? 1 : 0) || gd.ntiles <= 0) continue;
+          if (gd.taps_smem != want_smem || gd.win != want_win || gd.ntiles <= 0) continue;
           L.fuse_map[nm++] = (int8_t)gi;
           fsmem = std::max(fsmem, (size_t)gd.smem_bytes);
           ftiles = std::max(ftiles, (int)gd.ntiles);
         }
         if (nm == first) continue;
-        auto kern = pass == 0 ? poly_fp32_kernel<NB, true> : poly_fp32_kernel<NB, false>;
+        auto kern = want_win ? (want_smem ? poly_fp32_kernel<NB, true, true> : poly_fp32_kernel<NB, false, true>)
+                             : (want_smem ? poly_fp32_kernel<NB, true, false> : poly_fp32_kernel<NB, false, false>);
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
         if (e != cudaSuccess) return cuda_status(e);
         kern<<<dim3((unsigned)ftiles, (unsigned)(nm - first)), kThreads, fsmem, stream>>>(L, -1 - first);
@@ -808,7 +982,8 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
       if (st != FDSP_ERR_UNSUPPORTED) return st;
     }
     const size_t smem = (size_t)gd.smem_bytes;
-    auto kern = gd.taps_smem ? poly_fp32_kernel<NB, true> : poly_fp32_kernel<NB, false>;
+    auto kern = gd.win ? (gd.taps_smem ? poly_fp32_kernel<NB, true, true> : poly_fp32_kernel<NB, false, true>)
+                       : (gd.taps_smem ? poly_fp32_kernel<NB, true, false> : poly_fp32_kernel<NB, false, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e);
     kern<<<(unsigned)gd.ntiles, kThreads, smem, stream>>>(L, gi);

@@ -58,6 +58,8 @@ struct GroupDesc {
   int32_t meta_off;   // shared-memory offset (float2) of the staged channel constants
   int32_t smem_bytes; // dynamic shared memory of one CTA
   int32_t taps_smem;  // 1: taps staged in shared memory; 0: read through L1
+  int32_t win;        // 1: single-channel work sets, sliding-window rows (Qt multiple of 32 x kWinRows)
+  int32_t real_taps;  // 1: every tap of the group is real (2 FMAs per tap)
 };
 
 // One (tap batch, output class r) pair of a launch.  Output j of the class is
@@ -253,6 +255,9 @@ struct EngineGroup {
   int Qt;
   int Qt_default = 0;  // tile rows chosen from the shapes alone
   int use_tc = 1;      // tensor-core form when the precision asks for it (autotuned)
+  int win = 0;         // single-channel long filters: the FP32 kernel's sliding-window form applies
+  int Qt_win = 0;      // its tile rows (multiple of 32 x kWinRows)
+  int real_taps = 0;   // every channel of the group has real taps
   std::vector<int> batches;
 };
 
