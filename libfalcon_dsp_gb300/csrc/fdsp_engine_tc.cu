@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
   __shared__ __align__(8) uint64_t bar_d_full[kTcDSlots];    // accumulator ready  (commit)
   __shared__ __align__(8) uint64_t bar_d_empty[kTcDSlots];   // accumulator drained (one arrival per group warp)
   __shared__ __align__(8) uint64_t bar_b_full;               // B + slot constants (one arrival per producer warp)
-  __shared__ __align__(8) uint64_t bar_raw;                  // raw span landed    (bulk copy)
+  __shared__ __align__(8) uint64_t bar_raw[2];               // raw span landed    (bulk copy)
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane_id = tid & 31;
@@ -249,7 +249,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       tc::mbar_init(&bar_d_empty[i], 4);
     }
     tc::mbar_init(&bar_b_full, kTcProdThreads / 32);
-    tc::mbar_init(&bar_raw, 1);
+    tc::mbar_init(&bar_raw[0], 1);
+    tc::mbar_init(&bar_raw[1], 1);
     tc::mbar_fence_init();
   }
   tc::fence_before_sync();
@@ -352,35 +353,43 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     if (lane_id == 0) tc::mbar_arrive(&bar_b_full);
 
     if (L.raw_span > 0) {
-      // tiles through the raw buffer: one bulk copy brings the tile's whole
+      // tiles through the raw buffers: one bulk copy brings the tile's whole
       // input span; the three producer warps then write the records (v, q)
       // (phase D = phase 0 one row on) from shared memory, phases fastest
       // across threads (Qp is odd, so 8 consecutive records hit 8 distinct
-      // bank groups).  The next tile's copy is issued once the raw buffer
-      // has been read, so it overlaps the MMAs of this tile.
+      // bank groups).  With two raw buffers the copy of tile t + 2 is issued
+      // once tile t's span has been read, so copies stay one tile ahead of
+      // the record writes.
       const uint32_t raw_s = tc::smem_u32(smem + L.raw_off);
-      const uint2* raw = reinterpret_cast<const uint2*>(smem + L.raw_off);
+      const int nraw = L.nraw;
       const int64_t total = L.N + L.H;
       const int V = L.V, Qp = L.Qp;
       const TcSched S = tc_sched(L.nbuf);
       const int nrec = V * Qp;
       const int step_q = kTcProdThreads / V, step_v = kTcProdThreads % V;
-      bool pending = false;
-      if (tid == 0 && blockIdx.x < L.ntiles) raw_issue(L, (int64_t)blockIdx.x * 128 * D + L.B0 + L.H, raw_s, &bar_raw);
-      pending = blockIdx.x < L.ntiles;
+      int issued[2] = {0, 0}, landed[2] = {0, 0};  // copies per raw buffer
+      for (int i = 0; i < nraw; ++i) {
+        const int t = (int)blockIdx.x + i * (int)gridDim.x;
+        if (t < L.ntiles) {
+          if (tid == 0) raw_issue(L, (int64_t)t * 128 * D + L.B0 + L.H, raw_s + (uint32_t)(i * L.raw_stride), &bar_raw[i]);
+          issued[i]++;
+        }
+      }
       int tile_ord = 0;
       for (int tile = blockIdx.x; tile < L.ntiles; tile += gridDim.x, ++tile_ord) {
         int use = 0;
         const int buf = tc_buf(S, tile_ord, &use);
+        const int rb = tile_ord % nraw;
         const int64_t u0 = (int64_t)tile * 128 * D + L.B0 + L.H;
         const int64_t base = u0 & ~1LL;
-        bool ok = tc::mbar_wait_bounded(&bar_raw, (uint32_t)(tile_ord & 1), kWaitPolls);
-        if (ok) pending = false;
+        bool ok = tc::mbar_wait_bounded(&bar_raw[rb], (uint32_t)(landed[rb] & 1), kWaitPolls);
+        if (ok) landed[rb]++;
         if (ok && use >= 1) ok = tc::mbar_wait_bounded(&bar_in_empty[buf], (uint32_t)((use - 1) & 1), kWaitPolls);
         if (tc::named_bar_red_or(1, kTcProdThreads, !ok)) {
           failed = true;
           break;
         }
+        const uint2* raw = reinterpret_cast<const uint2*>(smem + L.raw_off + (size_t)rb * L.raw_stride);
         uint8_t* A = smem + L.in_off + (size_t)buf * L.in_bytes;
         int q = tid / V, v = tid - (tid / V) * V;
         for (int idx = tid; idx < nrec; idx += kTcProdThreads) {
@@ -395,22 +404,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
             ++q;
           }
         }
-        tc::named_bar_sync(1, kTcProdThreads);  // every read of the raw buffer is done
-        const int next = tile + (int)gridDim.x;
+        tc::named_bar_sync(1, kTcProdThreads);  // every read of raw buffer rb is done
+        const int next = tile + nraw * (int)gridDim.x;
         if (next < L.ntiles) {
           if (tid == 0) {
             tc::fence_proxy_async_smem();
-            raw_issue(L, (int64_t)next * 128 * D + L.B0 + L.H, raw_s, &bar_raw);
+            raw_issue(L, (int64_t)next * 128 * D + L.B0 + L.H, raw_s + (uint32_t)(rb * L.raw_stride), &bar_raw[rb]);
           }
-          pending = true;
+          issued[rb]++;
         }
         tc::fence_proxy_async_smem();  // the records are visible to the tensor core
         __syncwarp();
         if (lane_id == 0) tc::mbar_arrive(&bar_in_full[buf]);
       }
       if (failed) {
-        // a copy still in flight lands before the CTA can exit
-        if (pending) tc::mbar_wait_bounded(&bar_raw, (uint32_t)(tile_ord & 1), kWaitPolls);
+        // copies still in flight land before the CTA can exit
+        for (int i = 0; i < nraw; ++i)
+          for (; landed[i] < issued[i]; ++landed[i])
+            if (!tc::mbar_wait_bounded(&bar_raw[i], (uint32_t)(landed[i] & 1), kWaitPolls)) break;
         if (lane_id == 0) atomicExch(L.err, 1);
       }
     } else {
@@ -898,7 +909,8 @@ struct TcLaunchPlan {
   int64_t B0 = 0;
   int V = 0, Qp = 0, wrap = 0, nbuf = 1;
   int raw_span = 0;      // > 0: tiles staged through one bulk copy of their input span
-  size_t b_bytes = 0, meta_bytes = 0, tab_bytes = 0, in_bytes = 0, raw_bytes = 0;
+  int nraw = 0;          // raw span buffers (1 or 2)
+  size_t b_bytes = 0, meta_bytes = 0, tab_bytes = 0, in_bytes = 0, raw_bytes = 0, raw_stride = 0;
 };
 
 // [B of each merge set | slot constants | A-offset tables | raw span | input buffers]
@@ -907,7 +919,7 @@ size_t tc_smem_need(const TcLaunchPlan& p, int nbuf) {
 }
 
 // Staging geometry of a launch covering merge sets p.ms.
-void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t D, bool allow_raw = true) {
+void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t D, int raw_bufs = 2) {
   p.B0 = INT64_MAX;
   p.b_bytes = p.meta_bytes = p.tab_bytes = 0;
   p.nws = p.nslots = 0;
@@ -929,15 +941,18 @@ void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t
   // them with one bulk copy when the span is small enough (Qp odd keeps the
   // record writes free of bank conflicts)
   p.raw_span = 0;
-  p.raw_bytes = 0;
-  if (p.wrap && allow_raw) {
+  p.nraw = 0;
+  p.raw_bytes = p.raw_stride = 0;
+  if (p.wrap && raw_bufs > 0) {
     const int qp = p.Qp | 1;
     const size_t span = (size_t)qp * D + 1;
     const size_t bytes = (((span + 2) * 8) + 127) & ~(size_t)127;
     if (bytes <= kTcRawMax) {
       p.Qp = qp;
       p.raw_span = (int)span;
-      p.raw_bytes = bytes;
+      p.nraw = raw_bufs;
+      p.raw_stride = bytes;
+      p.raw_bytes = bytes * (size_t)raw_bufs;
     }
   }
   p.in_bytes = (((size_t)p.V * p.Qp * 16) + 127) & ~(size_t)127;
@@ -991,7 +1006,8 @@ bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, std::vector<TcLau
       TcLaunchPlan p = plans.back();
       p.ms.push_back(mi);
       tc_geometry(msets, p, D);
-      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, false);
+      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, 1);
+      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, 0);
       if (tc_smem_need(p, 1) <= kTcSmemMax && p.nws <= kMaxTcWorkSets && p.nslots <= kMaxTcSlots) {
         plans.back() = p;
         joined = true;
@@ -1001,7 +1017,8 @@ bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, std::vector<TcLau
       TcLaunchPlan p;
       p.ms.push_back(mi);
       tc_geometry(msets, p, D);
-      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, false);
+      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, 1);
+      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, 0);
       if (tc_smem_need(p, 1) > kTcSmemMax || p.nws > kMaxTcWorkSets || p.nslots > kMaxTcSlots) return false;
       plans.push_back(p);
     }
@@ -1156,6 +1173,8 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
     off = (off + 127) & ~(size_t)127;
     L.raw_off = (int32_t)off;
     L.raw_span = p.raw_span;
+    L.nraw = p.nraw;
+    L.raw_stride = (int32_t)p.raw_stride;
     off += p.raw_bytes;
     L.in_off = (int32_t)off;
     L.in_bytes = (int32_t)p.in_bytes;
