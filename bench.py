@@ -67,7 +67,7 @@ def parse():
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-other-configs", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
-    ap.add_argument("--serve-streams", type=int, default=8, help="concurrent streams the server admits")
+    ap.add_argument("--serve-streams", type=int, default=16, help="concurrent streams the server admits")
     return ap.parse_args()
 
 

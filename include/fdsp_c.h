@@ -369,7 +369,9 @@ int fdsp_polar_apply_host(fdsp_polar *h, const fdsp_cf32 *h_in, uint64_t n_in, f
  *     stream's filter history, resampler phase and NCO counter stay on the
  *     device between its blocks.
  *   - fdsp_server_submit enqueues one block on the stream's own CUDA stream
- *     (host->device copy, channelizer apply, device->host copies into h_out)
+ *     (host->device copy, channelizer apply, device->host copies into h_out;
+ *     a single copy when the h_out regions lie back to back, each at least
+ *     ceil(max_block * up / down) + 2 samples as given in out_cap)
  *     and returns a ticket at once; blocks of one stream run in order, blocks
  *     of different streams overlap on the GPU.  Host buffers should be pinned
  *     and must stay valid until the ticket completes.

@@ -51,7 +51,8 @@ struct ServeStream {
   fdsp_channelizer* ch = nullptr;
   cudaStream_t cs = nullptr;
   float2* d_in = nullptr;
-  std::vector<float2*> d_out;
+  float2* d_arena = nullptr;     // every channel's output, back to back (capacity each)
+  std::vector<float2*> d_out;    // channel c's part of the arena
   std::vector<uint64_t> cap;
   uint64_t max_block = 0;
   uint64_t footprint = 0;
@@ -75,8 +76,7 @@ void free_stream(ServeStream& s) {
   if (s.cs) cudaStreamSynchronize(s.cs);
   if (s.ch) fdsp_channelizer_destroy(s.ch);
   if (s.d_in) cudaFree(s.d_in);
-  for (auto p : s.d_out)
-    if (p) cudaFree(p);
+  if (s.d_arena) cudaFree(s.d_arena);
   if (s.cs) cudaStreamDestroy(s.cs);
   s = ServeStream();
 }
@@ -150,10 +150,13 @@ extern "C" int fdsp_server_open(fdsp_server* s, uint32_t fs, const fdsp_channel_
   if (rc == FDSP_OK) rc = cuda_status(cudaMalloc(&st.d_in, 8 * max_block));
   st.d_out.assign(nch, nullptr);
   st.cap.assign(nch, 0);
-  for (uint32_t c = 0; c < nch && rc == FDSP_OK; ++c) {
+  uint64_t total = 0;
+  for (uint32_t c = 0; c < nch; ++c) {
     st.cap[c] = (max_block * ch[c].up_rate + ch[c].down_rate - 1) / ch[c].down_rate + 2;
-    rc = cuda_status(cudaMalloc(&st.d_out[c], 8 * st.cap[c]));
+    total += st.cap[c];
   }
+  if (rc == FDSP_OK) rc = cuda_status(cudaMalloc(&st.d_arena, 8 * total));
+  for (uint32_t c = 0, off = 0; c < nch && rc == FDSP_OK; off += (uint32_t)st.cap[c], ++c) st.d_out[c] = st.d_arena + off;
   std::lock_guard<std::mutex> lk(s->mu);
   if (rc != FDSP_OK) {
     free_stream(st);
@@ -187,7 +190,16 @@ extern "C" int fdsp_server_submit(fdsp_server* s, uint32_t sid, const fdsp_cf32*
     rc = fdsp_channelizer_apply(st.ch, reinterpret_cast<const fdsp_cf32*>(st.d_in), n_in,
                                 reinterpret_cast<fdsp_cf32* const*>(st.d_out.data()), st.cap.data(), t->n_out.data(),
                                 (fdsp_stream_t)st.cs);
-  for (uint32_t c = 0; c < st.nch && rc == FDSP_OK; ++c) {
+  // host outputs laid out like the device arena (each channel's region at
+  // least the device capacity, back to back): one copy for the whole block
+  bool one_copy = out_cap != nullptr;
+  for (uint32_t c = 0; c < st.nch && one_copy; ++c)
+    one_copy = out_cap[c] >= st.cap[c] && h_out[c] == h_out[0] + (st.d_out[c] - st.d_arena);
+  if (one_copy && rc == FDSP_OK) {
+    const uint64_t n = (uint64_t)(st.d_out[st.nch - 1] - st.d_arena) + t->n_out[st.nch - 1];
+    rc = cuda_status(cudaMemcpyAsync(h_out[0], st.d_arena, 8 * n, cudaMemcpyDeviceToHost, st.cs));
+  }
+  for (uint32_t c = 0; c < st.nch && rc == FDSP_OK && !one_copy; ++c) {
     if (out_cap && out_cap[c] < t->n_out[c]) rc = FDSP_ERR_CAPACITY;
     if (rc == FDSP_OK && t->n_out[c])
       rc = cuda_status(cudaMemcpyAsync(h_out[c], st.d_out[c], 8 * t->n_out[c], cudaMemcpyDeviceToHost, st.cs));

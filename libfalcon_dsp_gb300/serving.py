@@ -34,6 +34,9 @@ class ChannelizerServer:
         self._h = C.c_void_p(0)
         _capi.call("fdsp_server_create", int(budget_bytes), int(max_active), C.byref(self._h))
         self._keep = {}
+        self._ticket = C.c_uint64()
+        self._ticket_ref = C.byref(self._ticket)
+        self._done, self._lat = C.c_int(), C.c_double()
 
     def __del__(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -73,19 +76,21 @@ class ChannelizerServer:
     def submit(self, sid: int, in_ptr: int, n_in: int, out_ptrs, out_caps) -> int:
         if not isinstance(out_ptrs, C.Array):
             out_ptrs, out_caps = self.out_args(out_ptrs, out_caps)
-        t = C.c_uint64()
-        st = _capi.lib().fdsp_server_submit(self._h, sid, in_ptr, n_in, out_ptrs, out_caps, C.byref(t))
+        t = self._ticket
+        st = _capi.lib().fdsp_server_submit(self._h, sid, in_ptr, n_in, out_ptrs, out_caps, self._ticket_ref)
         if st:
             _capi.check("fdsp_server_submit", st)
         return t.value
 
-    def poll(self, ticket: int, nch: int):
-        """(done, output counts, latency ms); a done ticket is reported once."""
-        done = C.c_int()
-        n_out = (C.c_uint64 * nch)()
-        lat = C.c_double()
-        _capi.call("fdsp_server_poll", self._h, int(ticket), C.byref(done), n_out, C.byref(lat))
-        return bool(done.value), list(n_out), lat.value
+    def poll(self, ticket: int, nch: int, n_out=None):
+        """(done, output counts, latency ms); a done ticket is reported once.
+        `n_out` may be a reused (c_uint64 * nch) array."""
+        if n_out is None:
+            n_out = (C.c_uint64 * nch)()
+        st = _capi.lib().fdsp_server_poll(self._h, ticket, C.byref(self._done), n_out, C.byref(self._lat))
+        if st:
+            _capi.check("fdsp_server_poll", st)
+        return bool(self._done.value), n_out, self._lat.value
 
     def wait_any(self, timeout_us: int = 1000) -> int:
         """Next completed ticket (0 when none completed within the timeout)."""
@@ -195,6 +200,7 @@ def run_serving(duration_s: float = 5.0, rate_hz: float = 2000.0, seed: int = 4,
                 off += 8 * c
             optr, ocap = ChannelizerServer.out_args(ptrs, caps)
             job.update(sid=sid, arena=arena, caps=ocap, ptrs=optr, left=job["blocks"],
+                       n_out=(C.c_uint64 * len(caps))(),
                        src=in_base + 8 * int(rng.integers(0, pool_n - job["block"])))
             wait_admit.append(time.perf_counter() - job["t_arrive"])
             t = srv.submit(sid, job["src"], job["block"], optr, ocap)
@@ -208,7 +214,7 @@ def run_serving(duration_s: float = 5.0, rate_hz: float = 2000.0, seed: int = 4,
         while t:
             sid = by_ticket.pop(t)
             job = active[sid]
-            srv.poll(t, len(job["channels"]))
+            srv.poll(t, len(job["channels"]), job["n_out"])
             if job["left"] > 0:
                 t2 = srv.submit(sid, job["src"], job["block"], job["ptrs"], job["caps"])
                 by_ticket[t2] = sid

@@ -25,7 +25,7 @@ def _caps(j):
     return [(j["block"] * c["up_rate"] + c["down_rate"] - 1) // c["down_rate"] + 2 for c in j["channels"]]
 
 
-def _run(jobs, max_active, precision):
+def _run(jobs, max_active, precision, contiguous=False):
     """Process every job's blocks in order; jobs run concurrently up to
     max_active (round-robin submission as each job's previous block ends)."""
     srv = ChannelizerServer(64 << 30, max_active)
@@ -52,7 +52,12 @@ def _run(jobs, max_active, precision):
                 del active[i]
                 continue
             caps = _caps(j)
-            a["bufs"] = [np.empty(c, np.complex64) for c in caps]
+            if contiguous:  # one host arena, channel regions back to back: the single-copy path
+                arena = np.empty(sum(caps), np.complex64)
+                offs = np.concatenate([[0], np.cumsum(caps)[:-1]])
+                a["bufs"] = [arena[o:o + c] for o, c in zip(offs, caps)]
+            else:
+                a["bufs"] = [np.empty(c, np.complex64) for c in caps]
             a["ticket"] = srv.submit(a["sid"], j["x"][a["k"]].ctypes.data, j["block"],
                                      [b.ctypes.data for b in a["bufs"]], caps)
             a["in"] = j["x"][a["k"]]
@@ -60,6 +65,16 @@ def _run(jobs, max_active, precision):
     st = srv.stats()
     assert st["active"] == 0 and st["used_bytes"] == 0
     return res
+
+
+def test_single_copy_outputs_equal_per_channel_copies():
+    jobs = _jobs(4, 21)
+    sep = _run(jobs, 4, 0)
+    one = _run(jobs, 4, 0, contiguous=True)
+    for i in range(len(jobs)):
+        for a, b in zip(sep[i], one[i]):
+            for u, v in zip(a, b):
+                assert np.array_equal(u, v)
 
 
 @pytest.mark.parametrize("precision", [0, 1])
