@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     }
     for (int i = 0; i < kTcDSlots; ++i) {
       tc::mbar_init(&bar_d_full[i], 1);
-      tc::mbar_init(&bar_d_empty[i], 4);
+      tc::mbar_init(&bar_d_empty[i], 16 / L.epi_groups);
     }
     tc::mbar_init(&bar_b_full, kTcProdThreads / 32);
     tc::mbar_init(&bar_raw[0], 1);
@@ -579,26 +579,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     if (failed && mw < S.nw && lane_id == 0) atomicExch(L.err, 1);
   } else {
     // ------------------------------------------------------------ epilogue
-    // Group eg drains items eg, eg+4, ... (item = tile_ord * nmsets + merge
-    // set; accumulator slot eg); warp w covers TMEM lanes 32 (w % 4) .. +31
-    // for every channel slot.  Each warp runs on its own (no barrier among
-    // epilogue warps), so a stop decision only has to be uniform over it.
-    const int eg = (warp - 4) >> 2;
+    // The 16 epilogue warps form NG groups (L.epi_groups: 4 for narrow merge
+    // sets, 1 for wide ones).  Group g owns the accumulator slots s with
+    // s % NG == g and drains their items in tile order (item = tile_ord *
+    // nmsets + merge set), so every slot keeps one in-order consumer.  Warp w
+    // covers TMEM lanes 32 (w % 4) .. +31 (the lanes it may read) and the
+    // 8-slot chunks cp, cp + 4/NG, ... of an item: with one group all 16
+    // warps share each item and a slot is free again after a quarter of its
+    // epilogue work; with four, each group's 4 warps drain whole items side
+    // by side.  Each warp runs on its own (a slot is released once the 16/NG
+    // warps of its group arrived), so a stop decision only has to be uniform
+    // over a warp.
+    const int NG = L.epi_groups;
+    const int mrow = (warp - 4) >> 2;
+    const int eg_own = mrow % NG;
+    const int cp = mrow / NG;
+    const int cstep = 4 / NG;
     const int quarter = warp & 3;
     const uint32_t lane = (uint32_t)(quarter * 32) << 16;
     const int row = quarter * 32 + lane_id;
     bool ok = tc::mbar_wait_bounded(&bar_b_full, 0u, kWaitPolls);
     if (__any_sync(0xffffffffu, !ok)) failed = true;
-    // slot eg belongs to MMA warp eg / spw; its items are that warp's items
-    // eg % spw, eg % spw + spw, ...
     const TcSched S = tc_sched(L.nbuf);
-    const int ew = eg / S.spw;
-    for (int jw = eg % S.spw; !failed; jw += S.spw) {
-      const int kt = jw / nms;
-      const int mi = jw - kt * nms;
-      const int tile_ord = kt * S.nw + ew;
+    for (int itg = 0; !failed; ++itg) {
+      const int tile_ord = itg / nms;
+      const int mi = itg - tile_ord * nms;
       const int tile = blockIdx.x + tile_ord * gridDim.x;
       if (tile >= L.ntiles) break;
+      // the accumulator slot of this item (the issuing warp's schedule)
+      const int ew = tile_ord % S.nw;
+      const int jw = (tile_ord / S.nw) * nms + mi;
+      const int eg = ew * S.spw + jw % S.spw;
+      if (eg % NG != eg_own) continue;  // another group's slot
       ok = tc::mbar_wait_bounded(&bar_d_full[eg], (uint32_t)((jw / S.spw) & 1), kWaitPolls);
       if (__any_sync(0xffffffffu, !ok)) {
         failed = true;
@@ -611,37 +623,39 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       const int nslots = M.N >> 1;
       const int64_t j0 = (int64_t)tile * 128;
       const int64_t j = j0 + row;
-      // row-0 NCO counter of the item for slots lane_id and lane_id + 32:
-      // P0 = (samples since reset at the window start of row 0) mod R; row
-      // `row` then starts at (P0 + row D) mod R: one subtraction unless the
-      // rollover is shorter than the tile
-      uint32_t p0a = 0, p0b = 0;
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int si = lane_id + 32 * h;
-        if (si < nslots && P0in[5 * nslots + si]) {
-          // x < R + 2^31 < 2^32 on the fast path; x >= -(T - 1) > -R
-          const int64_t x0 = (int64_t)(((uint64_t)P0in[nslots + si] << 32) | P0in[si]);
-          const int64_t x = x0 + j0 * D;
-          const uint32_t R = P0in[2 * nslots + si];
-          const uint64_t fm = ((uint64_t)P0in[4 * nslots + si] << 32) | P0in[3 * nslots + si];
-          const uint32_t pr0 = x < 0 ? (uint32_t)(x + R) : (uint32_t)__umul64hi(fm * (uint64_t)x, (uint64_t)R);
-          if (h == 0) p0a = pr0; else p0b = pr0;
-        }
-      }
       const uint32_t rowD = (uint32_t)(row * D);
       const int32_t j32 = (int32_t)j;
       const uint32_t dcol = (uint32_t)eg * kTcDCols;
       const int nch = M.N >> 4;  // 8-slot chunks (16 columns)
-      for (int cc = 0; cc < nch; ++cc) {
+      if (cp >= nch) {  // no chunk of this item for this warp: release at once
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane_id == 0) tc::mbar_arrive(&bar_d_empty[eg]);
+      }
+      for (int cc = cp; cc < nch; cc += cstep) {
         uint32_t v[16];
         tc::tmem_ld16(tbase + lane + dcol + 16 * cc, v);
         tc::tmem_wait_ld();
-        if (cc + 1 == nch) {
-          // the slot is free for the MMAs once every lane holds its last part
+        if (cc + cstep >= nch) {
+          // the slot is free for the MMAs once every warp holds its last part
           tc::fence_before_sync();
           __syncwarp();
           if (lane_id == 0) tc::mbar_arrive(&bar_d_empty[eg]);
+        }
+        // row-0 NCO counter of the chunk's 8 slots (lane e computes slot
+        // cc * 8 + e): P0 = (samples since reset at the window start of row
+        // 0) mod R; row `row` then starts at (P0 + row D) mod R
+        uint32_t p0 = 0;
+        {
+          const int si = cc * 8 + (lane_id & 7);
+          if (P0in[5 * nslots + si]) {
+            // x < R + 2^31 < 2^32 on the fast path; x >= -(T - 1) > -R
+            const int64_t x0 = (int64_t)(((uint64_t)P0in[nslots + si] << 32) | P0in[si]);
+            const int64_t x = x0 + j0 * D;
+            const uint32_t R = P0in[2 * nslots + si];
+            const uint64_t fm = ((uint64_t)P0in[4 * nslots + si] << 32) | P0in[3 * nslots + si];
+            p0 = x < 0 ? (uint32_t)(x + R) : (uint32_t)__umul64hi(fm * (uint64_t)x, (uint64_t)R);
+          }
         }
         // 8 slots branch free (their phase chains interleave), all results
         // computed before the stores; outputs whose window crosses the NCO
@@ -654,7 +668,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         for (int e = 0; e < 8; ++e) {
           const int si = cc * 8 + e;
           const TcSlotHot sh = hot[e];
-          const uint32_t P0 = __shfl_sync(0xffffffffu, si < 32 ? p0a : p0b, si & 31);
+          const uint32_t P0 = __shfl_sync(0xffffffffu, p0, e);
           const uint32_t R = sh.R;
           // (P0 + row D) mod R: P0 < R and row D < R - T on the fast path,
           // so one conditional subtraction
@@ -1096,6 +1110,11 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
     int nws = 0;
     int64_t rows = 0;
     L.nmsets = (int32_t)p.ms.size();
+    // wide merge sets (5 or more 8-slot chunks): all epilogue warps share
+    // each item; narrow ones: four groups drain whole items side by side
+    int max_n = 0;
+    for (int m : p.ms) max_n = std::max(max_n, ((msets[m].cols + 15) / 16) * 16);
+    L.epi_groups = (max_n / 16 >= 5) ? 1 : 4;
     for (size_t q = 0; q < p.ms.size(); ++q) {
       const TcMsetPlan& m = msets[p.ms[q]];
       TcMset& M = L.ms[q];

@@ -171,6 +171,7 @@ struct TcLaunch {
   int32_t raw_off;                   // shared-memory byte offset of the raw span buffer
   int32_t raw_span;                  // samples of a tile's raw span (0: per-record staging)
   int32_t nraw;                      // raw span buffers (1 or 2)
+  int32_t epi_groups;                // epilogue warp groups (1 or 4)
   int32_t raw_stride;                // bytes between raw span buffers
   TcMset ms[kMaxTcMsets];
   TcSlotHot slot[kMaxTcSlots];
