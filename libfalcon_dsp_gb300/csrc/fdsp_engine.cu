@@ -757,9 +757,11 @@ int PolyEngine::autotune(uint64_t n, cudaStream_t stream) {
   std::vector<float> best(ng, 3.4e38f), t;
   std::vector<int> best_qt(ng);
   for (size_t g = 0; g < ng; ++g) best_qt[g] = groups_[g].Qt_default;
-  // FP32 tile height: the default, half and double where shared memory allows
-  const int factor_num[3] = {1, 1, 2}, factor_den[3] = {1, 2, 1};
-  for (int ci = 0; ci < 3 && st == FDSP_OK; ++ci) {
+  // FP32 tile height: the default, half, double and four times where shared memory allows
+  // (large decimations start from small default tiles, where staging the
+  // input span and taps dominates: four times the default is tried too)
+  const int factor_num[4] = {1, 1, 2, 4}, factor_den[4] = {1, 2, 1, 1};
+  for (int ci = 0; ci < 4 && st == FDSP_OK; ++ci) {
     std::vector<char> valid(ng, 0);
     for (size_t g = 0; g < ng; ++g) {
       EngineGroup& eg = groups_[g];
