@@ -64,7 +64,7 @@ constexpr uint32_t kWaitPolls = 1u << 20;
 constexpr int kTcChunk = 32;          // channels per chunk (64 columns)
 constexpr int kTcMaxTaps = 64;        // taps per phase of a chunk
 constexpr int kTcMaxKw = 128;         // taps of a merged window
-constexpr size_t kTcSmemMax = 225 * 1024;
+constexpr size_t kTcSmemMax = 222 * 1024;  // + ~4.3 KB static (barriers, epilogue phasors) <= 227 KB
 constexpr int kTcMaxBuf = 4;          // input buffers
 constexpr size_t kTcRawMax = 48 * 1024; // raw span buffer (bulk-copy staging) at most
 
@@ -229,6 +229,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
   __shared__ __align__(8) uint64_t bar_d_empty[kTcDSlots];   // accumulator drained (one arrival per group warp)
   __shared__ __align__(8) uint64_t bar_b_full;               // B + slot constants (one arrival per producer warp)
   __shared__ __align__(8) uint64_t bar_raw[2];               // raw span landed    (bulk copy)
+  __shared__ __align__(16) float2 epi_ph[16 * 32];           // epilogue: one phasor per (slot, 8-row group) of a chunk
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane_id = tid & 31;
@@ -334,9 +335,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         // the row-0 counter inputs again, one array per field (lanes of the
         // epilogue read consecutive slots without bank conflicts): window
         // start of row 0 in samples since reset, R, the fast-modulo constant,
-        // and whether the slot rotates on the fast path
-        uint32_t* P0in = reinterpret_cast<uint32_t*>(smem + M.poff);
+        // whether the slot rotates on the fast path, its NCO step and T - 1
         const int NS = M.N >> 1;
+        float2* rtab = reinterpret_cast<float2*>(smem + M.poff);
+        uint32_t* P0in = reinterpret_cast<uint32_t*>(smem + M.poff + (size_t)NS * 64);
         const int64_t x0 = (int64_t)sm.nco.base + sm.delta - sm.T + 1;
         P0in[s] = (uint32_t)(uint64_t)x0;
         P0in[NS + s] = (uint32_t)((uint64_t)x0 >> 32);
@@ -344,6 +346,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         P0in[3 * NS + s] = (uint32_t)sm.fastmod;
         P0in[4 * NS + s] = (uint32_t)(sm.fastmod >> 32);
         P0in[5 * NS + s] = (sm.om_lo | sm.om_hi) ? 1u : 0u;
+        P0in[6 * NS + s] = sm.om_lo;
+        P0in[7 * NS + s] = sm.om_hi;
+        P0in[8 * NS + s] = sm.Tm1;
+        // rotation of row i of an 8-row group relative to the group's first
+        // row: e^{j 2 pi ((i D omega64) mod 2^64) / 2^64}, i = 0..7
+        for (int i = 0; i < 8; ++i) {
+          const uint32_t iD = (uint32_t)(i * D);
+          const uint32_t turns = __umulhi(iD, sm.om_lo) + iD * sm.om_hi;
+          float sn, cs;
+          sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);  // 2^-31
+          rtab[s * 8 + i] = make_float2(cs, sn);
+        }
       }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -619,8 +633,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       tc::fence_after_sync();
       const TcMset& M = L.ms[mi];
       const SlotMeta* meta = reinterpret_cast<const SlotMeta*>(smem + M.moff);
-      const uint32_t* P0in = reinterpret_cast<const uint32_t*>(smem + M.poff);
       const int nslots = M.N >> 1;
+      const float2* rtab = reinterpret_cast<const float2*>(smem + M.poff);
+      const uint32_t* P0in = reinterpret_cast<const uint32_t*>(smem + M.poff + (size_t)nslots * 64);
       const int64_t j0 = (int64_t)tile * 128;
       const int64_t j = j0 + row;
       const uint32_t rowD = (uint32_t)(row * D);
@@ -642,31 +657,64 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
           __syncwarp();
           if (lane_id == 0) tc::mbar_arrive(&bar_d_empty[eg]);
         }
-        // row-0 NCO counter of the chunk's 8 slots (lane e computes slot
-        // cc * 8 + e): P0 = (samples since reset at the window start of row
-        // 0) mod R; row `row` then starts at (P0 + row D) mod R
+        // row-0 NCO counter of the chunk's 8 slots (lane e + 8 g computes
+        // slot cc * 8 + e): P0 = (samples since reset at the window start of
+        // row 0) mod R; row `row` then starts at (P0 + row D) mod R
+        const int e_l = lane_id & 7;
+        const int si_l = cc * 8 + e_l;
         uint32_t p0 = 0;
+        const uint32_t R_l = P0in[2 * nslots + si_l];
+        if (P0in[5 * nslots + si_l]) {
+          // x < R + 2^31 < 2^32 on the fast path; x >= -(T - 1) > -R
+          const int64_t x0 = (int64_t)(((uint64_t)P0in[nslots + si_l] << 32) | P0in[si_l]);
+          const int64_t x = x0 + j0 * D;
+          const uint64_t fm = ((uint64_t)P0in[4 * nslots + si_l] << 32) | P0in[3 * nslots + si_l];
+          p0 = x < 0 ? (uint32_t)(x + R_l) : (uint32_t)__umul64hi(fm * (uint64_t)x, (uint64_t)R_l);
+        }
+        const TcSlotHot* hot = L.slot + M.slot0 + cc * 8;
+        // Grouped rotation: when no row of an 8-row group wraps the counter or
+        // has its window cross the rollover, the phase of row 8 g + i of the
+        // warp is the group's first-row phase plus i D omega (mod 1 turn), so
+        // the group needs one phasor (lane e + 8 g computes it for slot e) and
+        // the slot's table of the eight i D omega phasors.  Chunks where every
+        // group of every slot qualifies take this path.
         {
-          const int si = cc * 8 + (lane_id & 7);
-          if (P0in[5 * nslots + si]) {
-            // x < R + 2^31 < 2^32 on the fast path; x >= -(T - 1) > -R
-            const int64_t x0 = (int64_t)(((uint64_t)P0in[nslots + si] << 32) | P0in[si]);
-            const int64_t x = x0 + j0 * D;
-            const uint32_t R = P0in[2 * nslots + si];
-            const uint64_t fm = ((uint64_t)P0in[4 * nslots + si] << 32) | P0in[3 * nslots + si];
-            p0 = x < 0 ? (uint32_t)(x + R) : (uint32_t)__umul64hi(fm * (uint64_t)x, (uint64_t)R);
+          const uint32_t Tm1_l = P0in[8 * nslots + si_l];
+          const uint32_t rg = (uint32_t)(quarter * 32 + (lane_id & ~7)) * (uint32_t)D;  // first row of the group x D
+          uint32_t pg = p0 + rg;  // < R + 127 D < 2^32 on the fast path
+          pg = pg >= R_l ? pg - R_l : pg;
+          const bool fast_l = Tm1_l != 0x7fffffffu && pg + 7u * (uint32_t)D + Tm1_l < R_l;
+          if (__all_sync(0xffffffffu, fast_l)) {
+            const uint32_t turns = __umulhi(pg, P0in[6 * nslots + si_l]) + pg * P0in[7 * nslots + si_l];
+            float sn, cs;
+            __sincosf((float)(int32_t)turns * 1.4629180792671596e-09f, &sn, &cs);  // 2 pi / 2^32
+            float2* gph = epi_ph + (warp - 4) * 32;
+            gph[lane_id] = make_float2(cs, sn);
+            __syncwarp();
+            const float4* g4 = reinterpret_cast<const float4*>(gph + (lane_id & ~7));
+            const float2* rt = rtab + cc * 64 + (lane_id & 7);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+              const float4 a2 = g4[e >> 1];
+              const float2 A = (e & 1) ? make_float2(a2.z, a2.w) : make_float2(a2.x, a2.y);
+              const TcSlotHot& sh = hot[e];
+              const float2 y0 = make_float2(__uint_as_float(v[2 * e]), __uint_as_float(v[2 * e + 1]));
+              const float2 y = cmul_nco(y0, cmul_nco(A, rt[e * 8]));
+              float2* dst = reinterpret_cast<float2*>(((uint64_t)sh.out_hi << 32) | sh.out_lo) +
+                            (uint64_t)sh.U * (uint32_t)j32;
+              if (j32 < sh.J) *dst = y;
+            }
+            __syncwarp();  // every lane has read the phasors before the next chunk writes them
+            continue;
           }
         }
-        // 8 slots branch free (their phase chains interleave), all results
-        // computed before the stores; outputs whose window crosses the NCO
-        // rollover are written unrotated and fixed from that value below
-        uint32_t slow = 0, keep = 0;
-        float2 res[8];
-        uint64_t dst_a[8];
-        const TcSlotHot* hot = L.slot + M.slot0 + cc * 8;
+        // per-row rotation (a group wraps the counter or crosses the
+        // rollover, or a slot takes the exact path): outputs whose window
+        // crosses the NCO rollover are written unrotated and fixed from that
+        // value below
+        uint32_t slow = 0;
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
-          const int si = cc * 8 + e;
           const TcSlotHot sh = hot[e];
           const uint32_t P0 = __shfl_sync(0xffffffffu, p0, e);
           const uint32_t R = sh.R;
@@ -683,15 +731,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
           const float2 y0 = make_float2(__uint_as_float(v[2 * e]), __uint_as_float(v[2 * e + 1]));
           const float2 y = cmul_nco(y0, make_float2(cs, sn));
           const bool valid = j32 < sh.J;
-          const uint64_t m = (uint64_t)((sh.ur >> 16) & 0x7fffu) + (uint64_t)(sh.ur & 0xffffu) * (uint32_t)j32;
-          dst_a[e] = (((uint64_t)sh.out_hi << 32) | sh.out_lo) + m * sizeof(float2);
-          res[e] = okr ? y : y0;
-          keep |= valid ? (1u << e) : 0u;
+          float2* dst = reinterpret_cast<float2*>(((uint64_t)sh.out_hi << 32) | sh.out_lo) +
+                        (uint64_t)sh.U * (uint32_t)j32;
+          if (valid) *dst = okr ? y : y0;
           slow |= (valid && !okr) ? (1u << e) : 0u;
         }
-#pragma unroll
-        for (int e = 0; e < 8; ++e)
-          if (keep & (1u << e)) *reinterpret_cast<float2*>(dst_a[e]) = res[e];
         while (slow) {
           const int e = __ffs(slow) - 1;
           slow &= slow - 1;
@@ -943,7 +987,7 @@ void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t
     p.nws += (int)msets[m].ws.size();
     p.nslots += N / 2;
     p.b_bytes += (size_t)N * msets[m].Kw * 16;
-    p.meta_bytes += (size_t)(N / 2) * (sizeof(SlotMeta) + 6 * sizeof(uint32_t));
+    p.meta_bytes += (size_t)(N / 2) * (sizeof(SlotMeta) + 8 * sizeof(float2) + 9 * sizeof(uint32_t));
     p.tab_bytes += (size_t)((msets[m].Kw / 2 + 3) & ~3) * 4;
   }
   int64_t W = 0;
@@ -1165,11 +1209,12 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
                 nc.enabled && (nc.rollover >= 0x80000000u || 127LL * D + W.T >= (int64_t)nc.rollover);
             h.om_lo = nc.enabled && !general ? (uint32_t)nc.omega64 : 0u;
             h.om_hi = nc.enabled && !general ? (uint32_t)(nc.omega64 >> 32) : 0u;
-            h.out_lo = (uint32_t)(uintptr_t)out[c];
-            h.out_hi = (uint32_t)((uintptr_t)out[c] >> 32);
+            const uintptr_t o = (uintptr_t)(out[c] + W.r);
+            h.out_lo = (uint32_t)o;
+            h.out_hi = (uint32_t)(o >> 32);
             h.R = nc.enabled && !general ? nc.rollover : 0x7fffffffu;
             h.Tm1 = general ? 0x7fffffffu : (uint32_t)(W.T - 1);
-            h.ur = (uint32_t)W.U | ((uint32_t)W.r << 16);
+            h.U = (uint32_t)W.U;
             h.J = W.J;
           }
           break;
@@ -1180,7 +1225,7 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
       L.ms[q].moff = (int32_t)off;
       off += (size_t)(L.ms[q].N / 2) * sizeof(SlotMeta);
       L.ms[q].poff = (int32_t)off;
-      off += (size_t)(L.ms[q].N / 2) * 6 * sizeof(uint32_t);
+      off += (size_t)(L.ms[q].N / 2) * (8 * sizeof(float2) + 9 * sizeof(uint32_t));
     }
     L.tab_off = (int32_t)off;
     int toff = 0;

@@ -132,7 +132,7 @@ struct TcMset {
   int32_t ws_begin, ws_end;
   int32_t toff;          // first entry of its A-offset table (multiple of 4)
   int32_t slot0;         // first entry of its channel slots in TcLaunch::slot
-  int32_t poff;          // shared-memory byte offset of its row-0 counter inputs (one array per field)
+  int32_t poff;          // shared-memory byte offset of its row-rotation tables, then row-0 counter inputs
   int32_t pad_[2];
 };
 
@@ -141,10 +141,10 @@ struct TcMset {
 // shared-memory bandwidth from the matrix operands).
 struct TcSlotHot {
   uint32_t om_lo, om_hi;  // NCO turns per sample (2^-64 units; 0: no shift)
-  uint32_t out_lo, out_hi;// output base of the channel
+  uint32_t out_lo, out_hi;// output of row 0: channel output + r (row j writes out + U j)
   uint32_t R;             // counter rollover (0x7fffffff: no shift, or exact path)
   uint32_t Tm1;           // taps - 1 (0x7fffffff: every output on the exact path)
-  uint32_t ur;            // U | r << 16 (output m = r + U j)
+  uint32_t U;             // class up rate (output m = r + U j)
   int32_t J;              // rows with an output (0: padding slot)
 };
 
