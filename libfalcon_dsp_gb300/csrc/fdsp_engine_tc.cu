@@ -268,7 +268,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     for (int mi = 0; mi < nms; ++mi) {
       const TcMset& M = L.ms[mi];
       const int ncores = (M.N / 8) * M.Kw;
-      for (int p = tid; p < ncores * 8; p += kTcProdThreads) {
+      if (L.pair) {
+        // pair records: two matrices (hi taps, then lo taps) of cores
+        // (cg, m) of 8 columns x taps 2m, 2m + 1 at byte (cg Kw/2 + m) 128;
+        // column c at c 16, tap 2m + u at u 8 (the hi or lo half of the
+        // tap's 16-byte record)
+        const int half_k = M.Kw / 2;
+        const size_t mbytes = (size_t)(M.N / 8) * half_k * 128;
+        for (int p = tid; p < ncores * 16; p += kTcProdThreads) {
+          const int u = p & 1, c = (p >> 1) & 7;
+          const int rest = p >> 4;  // (h, cg, m)
+          const int m = rest % half_k;
+          const int hc = rest / half_k;
+          const int cg = hc % (M.N / 8), h = hc / (M.N / 8);
+          const int k = 2 * m + u;
+          const int slot = (cg * 8 + c) >> 1, part = c & 1;
+          uint8_t* dst = smem + M.boff + (size_t)h * mbytes + ((size_t)cg * half_k + m) * 128 + c * 16 + u * 8;
+          const uint8_t* src = nullptr;
+          for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
+            const TcWorkSet& W = L.ws[wi];
+            const int i = slot - W.s0;
+            if (i >= 0 && i < W.n && k >= W.o && k < W.o + W.T) {
+              src = W.b + ((size_t)(i >> 2) * W.T + (k - W.o)) * 128 + (2 * (i & 3) + part) * 16 + h * 8;
+              break;
+            }
+          }
+          if (src)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
+          else
+            *reinterpret_cast<uint2*>(dst) = make_uint2(0u, 0u);
+        }
+      }
+      for (int p = tid; p < (L.pair ? 0 : ncores * 8); p += kTcProdThreads) {
         const int core = p >> 3, piece = p & 7;
         const int cg = core / M.Kw, k = core - cg * M.Kw;
         const int slot = (cg * 8 + piece) >> 1, half = piece & 1;
@@ -378,6 +409,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       const int nraw = L.nraw;
       const int64_t total = L.N + L.H;
       const int V = L.V, Qp = L.Qp;
+      const bool pair = L.pair != 0;
       const TcSched S = tc_sched(L.nbuf);
       const int nrec = V * Qp;
       const int step_q = kTcProdThreads / V, step_v = kTcProdThreads % V;
@@ -407,10 +439,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         uint8_t* A = smem + L.in_off + (size_t)buf * L.in_bytes;
         int q = tid / V, v = tid - (tid / V) * V;
         for (int idx = tid; idx < nrec; idx += kTcProdThreads) {
-          const int64_t u = u0 + (v < D ? (int64_t)q * D + v : (int64_t)(q + 1) * D);
-          uint2 x = make_uint2(0u, 0u);
+          // phase D is phase 0 one row on; pair records hold samples 2v, 2v + 1
+          const int64_t u = u0 + (int64_t)q * D + (pair ? 2 * v : v);
+          uint2 x = make_uint2(0u, 0u), y = make_uint2(0u, 0u);
           if (u >= 0 && u < total) x = raw[u - base];
-          *reinterpret_cast<uint4*>(A + ((size_t)v * Qp + q) * 16) = make_uint4(x.x, x.y, x.x, x.y);
+          if (!pair)
+            y = x;
+          else if (u + 1 >= 0 && u + 1 < total)
+            y = raw[u + 1 - base];
+          *reinterpret_cast<uint4*>(A + ((size_t)v * Qp + q) * 16) = make_uint4(x.x, x.y, y.x, y.y);
           v += step_v;
           q += step_q;
           if (v >= V) {
@@ -453,6 +490,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
     const int V = L.V;
     const uint32_t half = (uint32_t)(tid & 1) * 8u;
     const int rsub = tid >> 1;  // 0..47
+    // record (v, q): sample q D + v in both halves, or (pair records) samples
+    // q D + 2 v and q D + 2 v + 1
+    const int vmul = L.pair ? 2 : 1;
+    const int hadd = L.pair ? (tid & 1) : 0;
     for (int tile = blockIdx.x; tile < L.ntiles; tile += gridDim.x, ++tile_ord) {
       int use = 0;
       const int buf = tc_buf(S, tile_ord, &use);
@@ -479,7 +520,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       const int64_t tb = (int64_t)tile * 128 * D + L.B0;
       for (int v = 0; v < V; ++v)
         for (int q = rsub; q < L.Qp; q += kTcProdThreads / 2)
-          stage_half(L, tb + (int64_t)q * D + v, xb + (uint32_t)(v * L.Qp + q) * 16u + half);
+          stage_half(L, tb + (int64_t)q * D + vmul * v + hadd, xb + (uint32_t)(v * L.Qp + q) * 16u + half);
       asm volatile("cp.async.commit_group;\n" ::: "memory");
       if (lag == 0) {
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -503,20 +544,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
   } else if (warp == 3 || warp == kTcThreads / 32 - 1) {
     // ------------------------------------------------------------ MMA issuer
     // A-offset table of every merge set: entry kp = record index (v Qp + q)
-    // of taps 2kp, 2kp+1 in a staged tile, i.e. the A descriptor's address
-    // field relative to the buffer (computed once, by all 32 lanes)
+    // of the first tap of MMA kp in a staged tile (taps 2kp, 2kp+1; with
+    // pair records taps 4kp .. 4kp+3, record phase v = tap phase / 2), i.e.
+    // the A descriptor's address field relative to the buffer (computed once,
+    // by all 32 lanes)
     const TcSched S = tc_sched(L.nbuf);
     const int mw = warp == 3 ? 0 : 1;
+    const int tpm = L.pair ? 4 : 2;  // taps per MMA
     uint32_t* tab = reinterpret_cast<uint32_t*>(smem + L.tab_off);
     for (int mi = 0; mi < nms && mw == 0; ++mi) {
       const TcMset& M = L.ms[mi];
-      const int nkp = M.Kw / 2;
+      const int nkp = M.Kw / tpm;
       for (int kp = lane_id; kp < ((nkp + 3) & ~3); kp += 32) {
         uint32_t e = 0;
         if (kp < nkp) {
-          const int s = M.a + 2 * kp;
+          const int s = M.a + tpm * kp;
           const int q = L.wrap ? s / D : 0;
-          e = (uint32_t)((s - q * D) * L.Qp + q);
+          e = (uint32_t)(((s - q * D) / (tpm / 2)) * L.Qp + q);
         }
         tab[M.toff + kp] = e;
       }
@@ -564,7 +608,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
           const uint32_t b_hi = (((uint32_t)M.Kw * 128u) >> 4) | (1u << 14);
           const uint32_t d_tm = tbase + ds * kTcDCols;
           const uint4* t4 = reinterpret_cast<const uint4*>(tab + M.toff);
-          const int nkp = M.Kw / 2;
+          if (L.pair) {
+            // pair records: MMA kp covers taps 4kp .. 4kp+3 (two records of
+            // two samples), once against the hi taps and once against the lo
+            // taps (B matrices of (N / 8) x (Kw / 2) cores, one after the
+            // other); both accumulate into the same columns
+            const uint32_t sbo = (((uint32_t)M.Kw / 2u * 128u) >> 4) | (1u << 14);
+            const uint32_t lo_off = ((uint32_t)M.N * (uint32_t)M.Kw * 8u) >> 4;
+            const int nkp = M.Kw / 4;
+            for (int kp = 0; kp < nkp; kp += 4) {
+              const uint4 o = t4[kp >> 2];
+              const uint32_t ao[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+              for (int i = 0; i < 4; ++i) {
+                if (kp + i < nkp) {
+                  const uint64_t da = ((uint64_t)a_hi << 32) | (a_lo0 + ao[i]);
+                  const uint32_t bl = b_lo0 + (uint32_t)(kp + i) * 16u;
+                  mma_ss(d_tm, da, ((uint64_t)sbo << 32) | bl, idesc, (kp + i) > 0 ? 1u : 0u);
+                  mma_ss(d_tm, da, ((uint64_t)sbo << 32) | (bl + lo_off), idesc, 1u);
+                }
+              }
+            }
+            tc::mma_commit(&bar_d_full[ds]);
+          }
+          const int nkp = L.pair ? 0 : M.Kw / 2;
           for (int kp = 0; kp < nkp; kp += 4) {
             // the four descriptor pairs are ready before the first MMA issues
             const uint4 o = t4[kp >> 2];
@@ -582,7 +649,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
             if (kp + 2 < nkp) mma_ss(d_tm, da2, db2, idesc, 1u);
             if (kp + 3 < nkp) mma_ss(d_tm, da3, db3, idesc, 1u);
           }
-          tc::mma_commit(&bar_d_full[ds]);
+          if (!L.pair) tc::mma_commit(&bar_d_full[ds]);
         }
         __syncwarp();
       }
@@ -966,6 +1033,7 @@ struct TcLaunchPlan {
   int nws = 0, nslots = 0;
   int64_t B0 = 0;
   int V = 0, Qp = 0, wrap = 0, nbuf = 1;
+  int pair = 0;          // 1: pair records (even D: 16-byte records of two samples)
   int raw_span = 0;      // > 0: tiles staged through one bulk copy of their input span
   int nraw = 0;          // raw span buffers (1 or 2)
   size_t b_bytes = 0, meta_bytes = 0, tab_bytes = 0, in_bytes = 0, raw_bytes = 0, raw_stride = 0;
@@ -978,6 +1046,7 @@ size_t tc_smem_need(const TcLaunchPlan& p, int nbuf) {
 
 // Staging geometry of a launch covering merge sets p.ms.
 void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t D, int raw_bufs = 2) {
+  const int tpm = p.pair ? 4 : 2;  // taps per MMA
   p.B0 = INT64_MAX;
   p.b_bytes = p.meta_bytes = p.tab_bytes = 0;
   p.nws = p.nslots = 0;
@@ -988,12 +1057,15 @@ void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t
     p.nslots += N / 2;
     p.b_bytes += (size_t)N * msets[m].Kw * 16;
     p.meta_bytes += (size_t)(N / 2) * (sizeof(SlotMeta) + 8 * sizeof(float2) + 9 * sizeof(uint32_t));
-    p.tab_bytes += (size_t)((msets[m].Kw / 2 + 3) & ~3) * 4;
+    p.tab_bytes += (size_t)((msets[m].Kw / tpm + 3) & ~3) * 4;
   }
   int64_t W = 0;
   for (int m : p.ms) W = std::max<int64_t>(W, msets[m].S - p.B0 + msets[m].Kw);
   p.wrap = W > (int64_t)D ? 1 : 0;
-  p.V = p.wrap ? (int)D + 1 : (int)W;
+  if (p.pair)
+    p.V = p.wrap ? (int)D / 2 + 1 : (int)W / 2;
+  else
+    p.V = p.wrap ? (int)D + 1 : (int)W;
   p.Qp = p.wrap ? 128 + (int)((W - 1) / D) : 128;
   // wrapped windows read (nearly) every sample of the tile's span: stage
   // them with one bulk copy when the span is small enough (Qp odd keeps the
@@ -1003,7 +1075,7 @@ void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t
   p.raw_bytes = p.raw_stride = 0;
   if (p.wrap && raw_bufs > 0) {
     const int qp = p.Qp | 1;
-    const size_t span = (size_t)qp * D + 1;
+    const size_t span = (size_t)qp * D + (p.pair ? 2 : 1);
     const size_t bytes = (((span + 2) * 8) + 127) & ~(size_t)127;
     if (bytes <= kTcRawMax) {
       p.Qp = qp;
@@ -1054,9 +1126,20 @@ std::vector<TcMsetPlan> tc_merge(const std::vector<TcWsPlan>& wl, const std::vec
   return msets;
 }
 
+// Pair records (even D) read taps four at a time from records of two
+// samples: every merged window starts on an even sample and spans a multiple
+// of four taps (the extra taps are zero).
+void tc_pair_windows(std::vector<TcMsetPlan>& msets) {
+  for (auto& m : msets) {
+    const int64_t S = m.S0 & ~1LL;  // even, at or before every work set's window start
+    m.Kw = (int)(((m.E - S + 1) + 3) & ~3LL);
+    m.S = S;
+  }
+}
+
 // Launches: consecutive merge sets while shared memory allows; false when a
 // single merge set does not fit.
-bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, std::vector<TcLaunchPlan>& plans) {
+bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, int pair, std::vector<TcLaunchPlan>& plans) {
   plans.clear();
   for (int mi = 0; mi < (int)msets.size(); ++mi) {
     bool joined = false;
@@ -1073,6 +1156,7 @@ bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, std::vector<TcLau
     }
     if (!joined) {
       TcLaunchPlan p;
+      p.pair = pair;
       p.ms.push_back(mi);
       tc_geometry(msets, p, D);
       if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, 1);
@@ -1120,10 +1204,12 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
   // and input tile do not fit in shared memory together
   std::vector<TcMsetPlan> msets;
   std::vector<TcLaunchPlan> plans;
+  const int pair = (D % 2 == 0) ? 1 : 0;  // records of two samples: half the staged bytes
   bool fits = false;
   for (int cap = (int)kTcDCols; cap >= 16 && !fits; cap /= 2) {
     msets = tc_merge(wl, order, cap);
-    fits = tc_pack(msets, D, plans);
+    if (pair) tc_pair_windows(msets);
+    fits = tc_pack(msets, D, pair, plans);
   }
   if (!fits) return FDSP_ERR_UNSUPPORTED;
   if (num_sms_ == 0) {
@@ -1231,7 +1317,7 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
     int toff = 0;
     for (size_t q = 0; q < p.ms.size(); ++q) {
       L.ms[q].toff = toff;
-      toff += (L.ms[q].Kw / 2 + 3) & ~3;
+      toff += (L.ms[q].Kw / (p.pair ? 4 : 2) + 3) & ~3;
     }
     off += (size_t)toff * 4;
     off = (off + 127) & ~(size_t)127;
@@ -1246,6 +1332,7 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
     L.V = p.V;
     L.Qp = p.Qp;
     L.wrap = p.wrap;
+    L.pair = p.pair;
     L.B0 = (int32_t)p.B0;
     L.ntiles = (int32_t)((rows + 127) / 128);
     if (L.ntiles == 0) continue;

@@ -173,6 +173,8 @@ struct TcLaunch {
   int32_t nraw;                      // raw span buffers (1 or 2)
   int32_t epi_groups;                // epilogue warp groups (1 or 4)
   int32_t raw_stride;                // bytes between raw span buffers
+  int32_t pair;                      // 1: records hold samples 2v, 2v + 1 of a phase pair (even D)
+  int32_t pad_;
   TcMset ms[kMaxTcMsets];
   TcSlotHot slot[kMaxTcSlots];
   TcWorkSet ws[kMaxTcWorkSets];
