@@ -206,6 +206,50 @@ __device__ __forceinline__ void raw_issue(const TcLaunch& L, int64_t u0, uint32_
   }
 }
 
+// Constants of channel slot s (columns 2s, 2s + 1) of merge set M: from the
+// work set that owns the slot, else a padding slot (J = 0).  Built once per
+// slot at CTA start (row-0 counter inputs) and again on the exact path.
+__device__ __noinline__ SlotMeta slot_meta(const TcLaunch& L, const TcMset& M, int s, int D) {
+  SlotMeta sm;
+  std::memset(&sm, 0, sizeof(sm));
+  sm.R = 0x7fffffffu;
+  for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
+    const TcWorkSet& W = L.ws[wi];
+    const int i = s - W.s0;
+    if (i < 0 || i >= W.n) continue;
+    const int c = W.ch[i];
+    const NcoConst nc = L.nco[c];
+    sm.nco.omega64 = nc.omega64;
+    sm.nco.wrap64 = nc.wrap64;
+    sm.nco.fastmod = nc.fastmod;
+    sm.nco.out = L.out[c];
+    sm.nco.rollover = nc.rollover;
+    sm.nco.base = L.nco_base[c];
+    sm.nco.enabled = nc.enabled;
+    // fast path: R < 2^31 (row counters in 32 bits) and 127 D + T < R, so
+    // the counter of row `row` is row 0's plus row D, past the rollover at
+    // most once (R >= 1e5 by construction, so this holds for D up to ~780);
+    // otherwise ("general") every output takes the exact path
+    const bool general = nc.enabled && (nc.rollover >= 0x80000000u || 127LL * D + W.T >= (int64_t)nc.rollover);
+    sm.fastmod = nc.fastmod;
+    sm.om_lo = nc.enabled && !general ? (uint32_t)nc.omega64 : 0u;
+    sm.om_hi = nc.enabled && !general ? (uint32_t)(nc.omega64 >> 32) : 0u;
+    sm.out = L.out[c];
+    sm.R = nc.enabled && !general ? nc.rollover : 0x7fffffffu;
+    sm.taps32 = W.taps32;
+    sm.delta = W.delta;
+    sm.T = W.T;
+    sm.Tm1 = general ? 0x7fffffffu : (uint32_t)(W.T - 1);
+    sm.U = W.U;
+    sm.r = W.r;
+    sm.J = W.J;
+    sm.tstride = W.n;
+    sm.tidx = i;
+    break;
+  }
+  return sm;
+}
+
 // D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
 __device__ __forceinline__ void mma_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                        uint32_t accumulate) {
@@ -320,50 +364,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       }
       // channel slot s = columns 2s, 2s+1
       for (int s = tid; s < M.N / 2; s += kTcProdThreads) {
-        SlotMeta sm;
-        std::memset(&sm, 0, sizeof(sm));
-        sm.R = 0x7fffffffu;
-        for (int wi = M.ws_begin; wi < M.ws_end; ++wi) {
-          const TcWorkSet& W = L.ws[wi];
-          const int i = s - W.s0;
-          if (i >= 0 && i < W.n) {
-            {
-              const int c = W.ch[i];
-              const NcoConst nc = L.nco[c];
-              sm.nco.omega64 = nc.omega64;
-              sm.nco.wrap64 = nc.wrap64;
-              sm.nco.fastmod = nc.fastmod;
-              sm.nco.out = L.out[c];
-              sm.nco.rollover = nc.rollover;
-              sm.nco.base = L.nco_base[c];
-              sm.nco.enabled = nc.enabled;
-              // fast path: R < 2^31 (row counters in 32 bits) and
-              // 127 D + T < R, so the counter of row `row` is row 0's plus
-              // row D, past the rollover at most once (R >= 1e5 by
-              // construction, so this holds for D up to ~780); otherwise
-              // ("general") every output takes the exact path
-              const bool general =
-                  nc.enabled && (nc.rollover >= 0x80000000u || 127LL * D + W.T >= (int64_t)nc.rollover);
-              sm.fastmod = nc.fastmod;
-              sm.om_lo = nc.enabled && !general ? (uint32_t)nc.omega64 : 0u;
-              sm.om_hi = nc.enabled && !general ? (uint32_t)(nc.omega64 >> 32) : 0u;
-              sm.out = L.out[c];
-              sm.R = nc.enabled && !general ? nc.rollover : 0x7fffffffu;
-              sm.taps32 = W.taps32;
-              sm.delta = W.delta;
-              sm.T = W.T;
-              sm.Tm1 = general ? 0x7fffffffu : (uint32_t)(W.T - 1);
-              sm.U = W.U;
-              sm.r = W.r;
-              sm.J = W.J;
-              sm.tstride = W.n;
-              sm.tidx = i;
-            }
-            break;
-          }
-        }
-        reinterpret_cast<SlotMeta*>(smem + M.moff)[s] = sm;
-        // the row-0 counter inputs again, one array per field (lanes of the
+        const SlotMeta sm = slot_meta(L, M, s, D);
+        // the slot's row-0 counter inputs, one array per field (lanes of the
         // epilogue read consecutive slots without bank conflicts): window
         // start of row 0 in samples since reset, R, the fast-modulo constant,
         // whether the slot rotates on the fast path, its NCO step and T - 1
@@ -699,7 +701,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       }
       tc::fence_after_sync();
       const TcMset& M = L.ms[mi];
-      const SlotMeta* meta = reinterpret_cast<const SlotMeta*>(smem + M.moff);
       const int nslots = M.N >> 1;
       const float2* rtab = reinterpret_cast<const float2*>(smem + M.poff);
       const uint32_t* P0in = reinterpret_cast<const uint32_t*>(smem + M.poff + (size_t)nslots * 64);
@@ -806,7 +807,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
         while (slow) {
           const int e = __ffs(slow) - 1;
           slow &= slow - 1;
-          const SlotMeta& sm = meta[cc * 8 + e];
+          const SlotMeta sm = slot_meta(L, M, cc * 8 + e, D);
           const int64_t w0 = (int64_t)sm.delta + j * D - sm.T + 1;
           float2* dst = sm.nco.out + ((int64_t)sm.r + (int64_t)sm.U * j);
           const ExactRot er = rotate_prep(sm.nco, w0, sm.T);
@@ -1056,7 +1057,7 @@ void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t
     p.nws += (int)msets[m].ws.size();
     p.nslots += N / 2;
     p.b_bytes += (size_t)N * msets[m].Kw * 16;
-    p.meta_bytes += (size_t)(N / 2) * (sizeof(SlotMeta) + 8 * sizeof(float2) + 9 * sizeof(uint32_t));
+    p.meta_bytes += (size_t)(N / 2) * (8 * sizeof(float2) + 9 * sizeof(uint32_t));
     p.tab_bytes += (size_t)((msets[m].Kw / tpm + 3) & ~3) * 4;
   }
   int64_t W = 0;
@@ -1308,8 +1309,6 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
       }
     }
     for (size_t q = 0; q < p.ms.size(); ++q) {
-      L.ms[q].moff = (int32_t)off;
-      off += (size_t)(L.ms[q].N / 2) * sizeof(SlotMeta);
       L.ms[q].poff = (int32_t)off;
       off += (size_t)(L.ms[q].N / 2) * (8 * sizeof(float2) + 9 * sizeof(uint32_t));
     }

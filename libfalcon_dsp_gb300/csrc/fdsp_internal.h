@@ -128,12 +128,11 @@ struct TcMset {
   int32_t N;             // MMA N: columns, multiple of 16, <= 128
   int32_t a;             // window start of row 0 inside the staged tile (records)
   int32_t boff;          // shared-memory byte offset of its B
-  int32_t moff;          // shared-memory byte offset of its channel-slot constants
   int32_t ws_begin, ws_end;
   int32_t toff;          // first entry of its A-offset table (multiple of 4)
   int32_t slot0;         // first entry of its channel slots in TcLaunch::slot
   int32_t poff;          // shared-memory byte offset of its row-rotation tables, then row-0 counter inputs
-  int32_t pad_[2];
+  int32_t pad_[3];
 };
 
 // Per-output constants of one channel slot, read by every output of the
