@@ -21,6 +21,13 @@
 // (hi + lo) x (hi + lo) complex product with FP32 accumulation in tensor
 // memory (~2^-22 relative, far above the 60 dB target).
 //
+// For even D the records are pairs instead: record (v, q) holds samples
+// q D + 2v and q D + 2v + 1 as {hi(re,im), lo(re,im)} each, so only phases
+// 0, 2, .., D are staged (half the bytes).  One MMA then covers four taps and
+// is issued twice, against a B of the hi taps and a B of the lo taps, into
+// the same accumulator columns; merged windows start on an even sample and
+// span a multiple of four taps.
+//
 // Work sets (class x output phase) of a group whose windows end close
 // together are merged into one product (a merge set): each one's taps sit at
 // its own offset of a common window (zeros elsewhere) and its channels side by
@@ -37,9 +44,10 @@
 //               and a drained accumulator slot, issues Kw/2 MMAs, commits;
 //   warps 4-19  epilogue, four groups of four warps (one per TMEM lane
 //               quarter); group g drains items g, g+4, ... (accumulator slot
-//               g): rotates by the exact integer NCO phase of each window
-//               start, fixes windows that straddle the NCO rollover with an
-//               exact FP32 split sum, and stores.
+//               g): rotates by the NCO phase of each window start (one
+//               phasor per 8-row group from the exact integer counter times
+//               a per-slot row-step table), fixes windows that straddle the
+//               NCO rollover with an exact FP32 split sum, and stores.
 // Every mbarrier wait is bounded and reports through an error flag.
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
