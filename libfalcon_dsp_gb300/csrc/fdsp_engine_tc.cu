@@ -718,12 +718,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) poly_tc_kernel(const __grid_con
       const int32_t j32 = (int32_t)j;
       const uint32_t dcol = (uint32_t)eg * kTcDCols;
       const int nch = M.N >> 4;  // 8-slot chunks (16 columns)
-      if (cp >= nch) {  // no chunk of this item for this warp: release at once
+      // the warps sharing an item take its chunks round robin, starting one
+      // column group further on every item, so the extra chunks of an item
+      // whose chunk count is not a multiple of four rotate over the warps
+      const int cpi = (cp + itg) % cstep;
+      if (cpi >= nch) {  // no chunk of this item for this warp: release at once
         tc::fence_before_sync();
         __syncwarp();
         if (lane_id == 0) tc::mbar_arrive(&bar_d_empty[eg]);
       }
-      for (int cc = cp; cc < nch; cc += cstep) {
+      for (int cc = cpi; cc < nch; cc += cstep) {
         uint32_t v[16];
         tc::tmem_ld16(tbase + lane + dcol + 16 * cc, v);
         tc::tmem_wait_ld();
