@@ -779,10 +779,26 @@ int PolyEngine::autotune(uint64_t n, cudaStream_t stream) {
   }
   for (size_t g = 0; g < ng; ++g) groups_[g].Qt = best_qt[g];
   if (st == FDSP_OK && precision_ != FDSP_PRECISION_FP32) {
-    st = run(1, t);
-    // a group keeps the tensor-core form only where that kernel really ran
-    // (configurations beyond its limits fall back to FP32) and was faster
-    for (size_t g = 0; g < ng && st == FDSP_OK; ++g) groups_[g].use_tc = (prof_tc_[g] && t[g] < best[g]) ? 1 : 0;
+    // tensor-core form with row splits of up to 1, 2 and 4 (groups with few
+    // channel columns); a group keeps the tensor-core form only where that
+    // kernel really ran (configurations beyond its limits fall back to FP32)
+    // and was faster
+    std::vector<int> best_split(ng, 1), use(ng, 0);
+    const int splits[3] = {1, 2, 4};
+    for (int si = 0; si < 3 && st == FDSP_OK; ++si) {
+      for (size_t g = 0; g < ng; ++g) groups_[g].tc_split = splits[si];
+      st = run(1, t);
+      for (size_t g = 0; g < ng && st == FDSP_OK; ++g)
+        if (prof_tc_[g] && t[g] < best[g]) {
+          best[g] = t[g];
+          best_split[g] = splits[si];
+          use[g] = 1;
+        }
+    }
+    for (size_t g = 0; g < ng; ++g) {
+      groups_[g].use_tc = use[g];
+      groups_[g].tc_split = best_split[g];
+    }
   }
   force_ = -1;
   for (auto ev : prof_ev_)

@@ -909,7 +909,7 @@ int PolyEngine::build_tc(int fmt) {
       const int n = (int)ch.chans.size();
       const int tmax = (int)chans_[ch.chans[0]].T;
       ch.T = (tmax + 1) & ~1;
-      ch.supported = ch.T <= kTcMaxTaps && k.up < 32768u;  // U and r packed in 16 / 15 bits
+      ch.supported = ch.T <= kTcMaxTaps;
       ch.ng = (2 * n + 7) / 8;
       ch.bbytes = (size_t)ch.ng * ch.T * 128;
       ch.d_b = nullptr;
@@ -1189,24 +1189,47 @@ bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, int pair, std::ve
 
 int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream) {
   const EngineGroup& g = groups_[gi];
-  const uint32_t D = g.D;
-  // ---- work sets of this apply (chunk x output phase r)
+  const uint32_t Dg = g.D;
+  // Row split: a group with few channel columns wastes most of each MMA's N.
+  // Its work sets' rows j = S i + b (b < S) become S work sets whose rows
+  // are S D samples apart and whose windows end b D later; merged, one
+  // staged tile then feeds S x the columns (the window grows by (S - 1) D
+  // taps, the MMAs per output drop by about S, B grows S-fold).  S is the
+  // largest split up to the group's limit (autotuned) whose columns and
+  // window still fit one merge set.
+  int cols = 0, tmax = 0;
+  for (const auto& ch : tc_chunks_) {
+    const EngineClass& k = classes_[ch.cls];
+    if (k.down != Dg || !ch.supported) continue;
+    cols += 2 * (int)ch.chans.size() * (int)k.up;
+    tmax = std::max(tmax, ch.T);
+  }
+  uint32_t split = 1;
+  while ((int)split < g.tc_split && cols > 0 && cols * (int)(split + 1) <= (int)kTcDCols &&
+         (int64_t)tmax + (int64_t)split * Dg + 4 <= kTcMaxKw)
+    ++split;
+  const uint32_t D = Dg * split;
+  // ---- work sets of this apply (chunk x output phase r x row class b)
   std::vector<TcWsPlan> wl;
   for (const auto& ch : tc_chunks_) {
     const EngineClass& k = classes_[ch.cls];
-    if (k.down != D) continue;
+    if (k.down != Dg) continue;
     const uint32_t U = k.up;
     for (uint32_t r = 0; r < U; ++r) {
       if (k.M <= r) continue;
-      const uint64_t t = (uint64_t)k.phase + (uint64_t)r * D;
-      TcWsPlan w;
-      w.ch = &ch;
-      w.phi = (uint32_t)(t % U);
-      w.delta = (int64_t)(k.xoffset + t / U);
-      w.J = (int64_t)((k.M - r + U - 1) / U);
-      w.U = U;
-      w.r = r;
-      wl.push_back(w);
+      const uint64_t t = (uint64_t)k.phase + (uint64_t)r * Dg;
+      const int64_t J = (int64_t)((k.M - r + U - 1) / U);
+      for (uint32_t b = 0; b < split; ++b) {
+        if (J <= (int64_t)b) continue;
+        TcWsPlan w;
+        w.ch = &ch;
+        w.phi = (uint32_t)(t % U);
+        w.delta = (int64_t)(k.xoffset + t / U) + (int64_t)b * Dg;
+        w.J = (J - (int64_t)b + split - 1) / split;
+        w.U = U * split;
+        w.r = r + b * U;
+        wl.push_back(w);
+      }
     }
   }
   if (wl.empty()) return FDSP_OK;

@@ -259,6 +259,7 @@ struct EngineGroup {
   int Qt;
   int Qt_default = 0;  // tile rows chosen from the shapes alone
   int use_tc = 1;      // tensor-core form when the precision asks for it (autotuned)
+  int tc_split = 1;    // largest row split of the tensor-core form (autotuned; 1 = none)
   int win = 0;         // single-channel long filters: the FP32 kernel's sliding-window form applies
   int Qt_win = 0;      // its tile rows (multiple of 32 x kWinRows)
   int real_taps = 0;   // every channel of the group has real taps
