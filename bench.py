@@ -491,7 +491,8 @@ def run_ours(args) -> None:
                        "path": {"fp32": "plain FP32 SIMT",
                                 "fp16x3": "tensor cores (tcgen05), FP16 (hi+lo)(hi+lo), FP32 accumulate",
                                 "bf16x3": "tensor cores (tcgen05), BF16 (hi+lo)(hi+lo), FP32 accumulate"}[args.precision],
-                       "autotune": [{"down": t["down_rate"], "tile_rows": t["tile_rows"], "tc": t["tensor_core"]}
+                       "autotune": [{"down": t["down_rate"], "tile_rows": t["tile_rows"], "tc": t["tensor_core"],
+                                     "tc_split": t["tc_split"]}
                                     for t in tune],
                        "cuda_graph": not args.no_graph, "graph_replays": ch.graph_replays(),
                        "l2": "no flush: each step reads 512 MiB and writes ~9.6 GB, far above the 129 MB L2",

@@ -233,9 +233,11 @@ class MultiRateChannelizerCuda(_Handle):
         _capi.call("fdsp_channelizer_num_groups", self._h, C.byref(n))
         out = []
         for g in range(n.value):
-            d, q, tcf = C.c_uint32(), C.c_uint32(), C.c_int()
+            d, q, tcf, sp = C.c_uint32(), C.c_uint32(), C.c_int(), C.c_uint32()
             _capi.call("fdsp_channelizer_group_info", self._h, g, C.byref(d), C.byref(q), C.byref(tcf))
-            out.append({"down_rate": d.value, "tile_rows": q.value, "tensor_core": bool(tcf.value)})
+            _capi.call("fdsp_channelizer_group_tc_split", self._h, g, C.byref(sp))
+            out.append({"down_rate": d.value, "tile_rows": q.value, "tensor_core": bool(tcf.value),
+                        "tc_split": sp.value})
         return out
 
     def tc_groups(self) -> int:

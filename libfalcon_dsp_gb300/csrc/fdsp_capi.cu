@@ -268,6 +268,13 @@ int fdsp_channelizer_group_info(const fdsp_channelizer* h, uint32_t group, uint3
   return FDSP_OK;
 }
 
+int fdsp_channelizer_group_tc_split(const fdsp_channelizer* h, uint32_t group, uint32_t* split) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!split || group >= (uint32_t)h->eng.num_groups()) return FDSP_ERR_INVALID_ARG;
+  *split = (uint32_t)h->eng.group_tc_split((int)group);
+  return FDSP_OK;
+}
+
 int fdsp_channelizer_apply_host(fdsp_channelizer* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_cf32* const* h_out,
                                 const uint64_t* out_cap, uint64_t* n_out, fdsp_stream_t stream) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;

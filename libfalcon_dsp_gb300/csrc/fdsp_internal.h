@@ -321,6 +321,7 @@ class PolyEngine {
     *Qt = groups_[g].Qt;
     *use_tc = use_tc_for(g) ? 1 : 0;
   }
+  int group_tc_split(int g) const { return groups_[g].tc_split; }
 
  private:
   template <int NB>
