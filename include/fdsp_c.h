@@ -209,9 +209,9 @@ int fdsp_channelizer_set_graph(fdsp_channelizer *h, int enable);
 int fdsp_channelizer_graph_replays(const fdsp_channelizer *h, uint32_t *replays);
 int fdsp_channelizer_group_info(const fdsp_channelizer *h, uint32_t group, uint32_t *down_rate, uint32_t *tile_rows,
                                 int *tensor_core);
-/* Largest row split S of a group's tensor-core form (autotuned among 1, 2,
- * 4; 1 = none): rows j = S i + b run as S work sets at stride S x down_rate,
- * so one staged tile feeds S times the channel columns. */
+/* Row split S of a group's last tensor-core launch (1 = none; its limit is
+ * autotuned among 1, 2, 4): rows j = S i + b run as S work sets at stride
+ * S x down_rate, so one staged tile feeds S times the channel columns. */
 int fdsp_channelizer_group_tc_split(const fdsp_channelizer *h, uint32_t group, uint32_t *split);
 /* apply(in, out) on host buffers (copies in, computes, copies out, syncs). */
 int fdsp_channelizer_apply_host(fdsp_channelizer *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,

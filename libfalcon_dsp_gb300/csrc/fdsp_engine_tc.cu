@@ -1209,6 +1209,7 @@ int PolyEngine::launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* 
          (int64_t)tmax + (int64_t)split * Dg + 4 <= kTcMaxKw)
     ++split;
   const uint32_t D = Dg * split;
+  groups_[gi].tc_split_used = (int)split;
   // ---- work sets of this apply (chunk x output phase r x row class b)
   std::vector<TcWsPlan> wl;
   for (const auto& ch : tc_chunks_) {

@@ -260,6 +260,7 @@ struct EngineGroup {
   int Qt_default = 0;  // tile rows chosen from the shapes alone
   int use_tc = 1;      // tensor-core form when the precision asks for it (autotuned)
   int tc_split = 1;    // largest row split of the tensor-core form (autotuned; 1 = none)
+  int tc_split_used = 1;  // row split of its last tensor-core launch
   int win = 0;         // single-channel long filters: the FP32 kernel's sliding-window form applies
   int Qt_win = 0;      // its tile rows (multiple of 32 x kWinRows)
   int real_taps = 0;   // every channel of the group has real taps
@@ -321,7 +322,7 @@ class PolyEngine {
     *Qt = groups_[g].Qt;
     *use_tc = use_tc_for(g) ? 1 : 0;
   }
-  int group_tc_split(int g) const { return groups_[g].tc_split; }
+  int group_tc_split(int g) const { return groups_[g].tc_split_used; }
 
  private:
   template <int NB>
