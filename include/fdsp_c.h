@@ -213,6 +213,10 @@ int fdsp_channelizer_group_info(const fdsp_channelizer *h, uint32_t group, uint3
  * autotuned among 1, 2, 4): rows j = S i + b run as S work sets at stride
  * S x down_rate, so one staged tile feeds S times the channel columns. */
 int fdsp_channelizer_group_tc_split(const fdsp_channelizer *h, uint32_t group, uint32_t *split);
+/* Largest row split (1..8) of every group's tensor-core form until the next
+ * autotune; the split used is the largest one up to it whose columns
+ * (<= 128) and merged window (<= 128 taps) fit one product. */
+int fdsp_channelizer_set_tc_split(fdsp_channelizer *h, uint32_t max_split);
 /* apply(in, out) on host buffers (copies in, computes, copies out, syncs). */
 int fdsp_channelizer_apply_host(fdsp_channelizer *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,
                                 const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);

@@ -205,6 +205,12 @@ class MultiRateChannelizerCuda(_Handle):
         FP32 accumulation)."""
         _capi.call("fdsp_channelizer_set_precision", self._h, self.PRECISION[mode])
 
+    def set_tc_split(self, max_split: int) -> None:
+        """Largest row split (1..8) of the tensor-core form: a group's rows
+        j = S i + b run as S work sets at stride S x down_rate, so one staged
+        tile feeds S times the channel columns.  autotune() sets it per group."""
+        _capi.call("fdsp_channelizer_set_tc_split", self._h, int(max_split))
+
     def kernel_launches(self) -> int:
         v = C.c_uint32()
         _capi.call("fdsp_channelizer_kernel_launches", self._h, C.byref(v))

@@ -100,6 +100,7 @@ SIGNATURES = {
     "fdsp_channelizer_graph_replays": [_vp, _pu32],
     "fdsp_channelizer_group_info": [_vp, _u32, _pu32, _pu32, C.POINTER(C.c_int)],
     "fdsp_channelizer_group_tc_split": [_vp, _u32, _pu32],
+    "fdsp_channelizer_set_tc_split": [_vp, _u32],
     "fdsp_channelizer_set_precision": [_vp, C.c_int],
     "fdsp_resampler_create": [_u32, _u32, _vp, _u32, _pp],
     "fdsp_resampler_destroy": [_vp],

@@ -268,6 +268,11 @@ int fdsp_channelizer_group_info(const fdsp_channelizer* h, uint32_t group, uint3
   return FDSP_OK;
 }
 
+int fdsp_channelizer_set_tc_split(fdsp_channelizer* h, uint32_t max_split) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return h->eng.set_tc_split((int)max_split);
+}
+
 int fdsp_channelizer_group_tc_split(const fdsp_channelizer* h, uint32_t group, uint32_t* split) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
   if (!split || group >= (uint32_t)h->eng.num_groups()) return FDSP_ERR_INVALID_ARG;

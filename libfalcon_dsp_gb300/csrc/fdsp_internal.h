@@ -307,8 +307,9 @@ class PolyEngine {
   // 1 when a tensor-core kernel hit its bounded wait since the last reset.
   int tc_error() const;
   // Time every decimation group on an n-sample block: the FP32 tile height
-  // among {1/2, 1, 2} x the default, then tensor cores vs FP32 under a
-  // tensor-core precision; keep the fastest per group.  Resets the stream.
+  // among {1/2, 1, 2, 4} x the default, then tensor cores (row split of up
+  // to 1, 2, 4) vs FP32 under a tensor-core precision; keep the fastest per
+  // group.  Resets the stream.
   int autotune(uint64_t n, cudaStream_t stream);
   int num_groups() const { return (int)groups_.size(); }
   // CUDA-graph replay of each apply's launch sequence (captured on the
@@ -323,6 +324,13 @@ class PolyEngine {
     *use_tc = use_tc_for(g) ? 1 : 0;
   }
   int group_tc_split(int g) const { return groups_[g].tc_split_used; }
+  // Largest row split of every group's tensor-core form (1..8); the
+  // autotuner sets it per group.
+  int set_tc_split(int s) {
+    if (s < 1 || s > 8) return FDSP_ERR_INVALID_ARG;
+    for (auto& g : groups_) g.tc_split = s;
+    return FDSP_OK;
+  }
 
  private:
   template <int NB>

@@ -74,6 +74,31 @@ def test_tc_rollover_straddles_and_matches_fp32_path():
                 assert snr_db(ya, yc) >= 100.0
 
 
+@pytest.mark.parametrize("split", [2, 4])
+def test_tc_row_split_matches_fp64(split):
+    """Row split (rows j = S i + b of a work set run as S work sets at stride
+    S D, merged into one product): within the tensor-core bound of the FP64
+    oracle over a streaming sequence whose windows straddle NCO rollovers,
+    with the split each group used reported by group_info."""
+    fs = 1000000
+    chans = [dict(freq_shift_in_hz=f, up_rate=u, down_rate=d, coeffs=_rand(u * t, 30 + i, 0.05).real.astype(np.complex64))
+             for i, (f, u, d, t) in enumerate([(100000, 1, 4, 64), (-100000, 3, 8, 40), (12345, 2, 25, 33),
+                                               (250000, 1, 8, 12), (-1, 3, 16, 57), (0, 1, 4, 20)])]
+    x = _rand(300000, 31)
+    g = F.MultiRateChannelizerCuda(fs, chans)
+    g.set_precision("fp16x3")
+    g.set_tc_split(split)
+    o64 = O.Channelizer(fs, chans, precision="f64")
+    for i, j in [(0, 777), (777, 100001), (100001, 300000)]:
+        for yb, yc in zip(g.apply(x[i:j]), o64.apply(x[i:j])):
+            assert yb.size == yc.size
+            if yc.size > 8:
+                assert snr_db(yb, yc) >= SNR_MIN_DB, snr_db(yb, yc)
+    used = [gi["tc_split"] for gi in g.group_info()]
+    assert max(used) == split and min(used) >= 1, used
+    assert g.tc_groups() == len(used)
+
+
 def test_autotune_keeps_results_and_streaming():
     """The autotuner only picks tile heights and forms: outputs after it stay
     within the tensor-core bound of the FP64 oracle, from a reset state, and
