@@ -279,7 +279,10 @@ int fdsp_resampler_apply_ci16(fdsp_resampler *h, const int16_t *d_in, uint64_t n
  *     address; make it before any stream capture begins.
  *   - coeffs may be a host or a device pointer; it is copied in stream
  *     order, so pinned or device taps must stay unchanged until the stream
- *     reaches the call.
+ *     reaches the call.  Inside a CUDA graph capture only device or pinned
+ *     taps work: a copy from pageable host memory cannot be captured.
+ *   - The array's address is looked up once per device and kept for the
+ *     life of the process; calls must not span a cudaDeviceReset.
  *   - The array is shared by every call on the device and keeps the last
  *     call's taps: calls that overlap in time (different streams or host
  *     threads without ordering) race on it.  Serialise them.

@@ -1,10 +1,9 @@
 /*
  * Drop-in for libfalcon_dsp's falcon_dsp_fm_demodulator_cuda
- * (hdr/signals/falcon_dsp_fm_demod_cuda.h:83-104): initialize(input rate,
- * offset of the station from DC, de-emphasis time constant), reset_state(),
- * demod_mono(complex block -> int16 mono audio at 45.6 kS/s).  Every stage
- * (channelizer, discriminator, de-emphasis, mono decimator, rescale) runs on
- * the GPU; the reference runs all but the first on the CPU.  The constants
+ * (hdr/signals/falcon_dsp_fm_demod_cuda.h:83-104).  As in the reference it
+ * derives from falcon_dsp_fm_demodulator (falcon_dsp_fm_demod.h here,
+ * GPU-backed too) and overrides initialize, reset_state and demod_mono, so
+ * it can be used through a base-class reference or pointer.  The constants
  * are those of hdr/signals/falcon_dsp_fm_demod.h:96-100.
  */
 #ifndef FALCON_DSP_FM_DEMOD_CUDA_H
@@ -14,59 +13,26 @@
 #include <cstdint>
 #include <vector>
 
-#include "../transform/falcon_dsp_gb300_detail.h"
+#include "falcon_dsp_fm_demod.h"
 
 namespace falcon_dsp {
 
-class falcon_dsp_fm_demodulator_cuda {
+class falcon_dsp_fm_demodulator_cuda : public falcon_dsp_fm_demodulator {
 public:
-    static constexpr float AMERICAS_FM_DEEMPHASIS_TIME_CONSTANT = 75e-6;
-    static constexpr float EUROPE_ASIA_FM_DEEMPHASIS_TIME_CONSTANT = 50e-6;
-    static const uint32_t FM_RADIO_SAMPLE_RATE_IN_SPS = 228000;
-    static const uint32_t FM_RADIO_AUDIO_SAMPLE_RATE_IN_SPS = 45600;
-
     falcon_dsp_fm_demodulator_cuda(void) = default;
-    virtual ~falcon_dsp_fm_demodulator_cuda(void) {
-        if (m_h) fdsp_fm_demod_destroy(m_h);
-    }
+    ~falcon_dsp_fm_demodulator_cuda(void) override = default;
     falcon_dsp_fm_demodulator_cuda(const falcon_dsp_fm_demodulator_cuda&) = delete;
     falcon_dsp_fm_demodulator_cuda& operator=(const falcon_dsp_fm_demodulator_cuda&) = delete;
 
-    /* Once only; false for an unsupported time constant or an input rate
-     * without a predefined 228 kS/s filter, as the reference. */
-    virtual bool initialize(uint32_t input_sample_rate_in_sps, int32_t signal_offset_from_dc_in_hz,
-                            float deemphasis_time_constant_in_usecs = AMERICAS_FM_DEEMPHASIS_TIME_CONSTANT) {
-        if (m_h) return false;
-        if (fdsp_fm_demod_create(input_sample_rate_in_sps, signal_offset_from_dc_in_hz,
-                                 deemphasis_time_constant_in_usecs, &m_h) != FDSP_OK) {
-            m_h = nullptr;
-            return false;
-        }
-        return true;
+    bool initialize(uint32_t input_sample_rate_in_sps, int32_t signal_offset_from_dc_in_hz,
+                    float deemphasis_time_constant_in_usecs = AMERICAS_FM_DEEMPHASIS_TIME_CONSTANT) override {
+        return falcon_dsp_fm_demodulator::initialize(input_sample_rate_in_sps, signal_offset_from_dc_in_hz,
+                                                     deemphasis_time_constant_in_usecs);
     }
-
-    virtual void reset_state(void) {
-        if (m_h) fdsp_fm_demod_reset(m_h);
+    void reset_state(void) override { falcon_dsp_fm_demodulator::reset_state(); }
+    bool demod_mono(std::vector<std::complex<float>>& in, std::vector<int16_t>& out) override {
+        return falcon_dsp_fm_demodulator::demod_mono(in, out);
     }
-
-    virtual bool demod_mono(std::vector<std::complex<float>>& in, std::vector<int16_t>& out) {
-        out.clear();
-        if (!m_h) return false;
-        uint64_t n = 0;
-        if (fdsp_fm_demod_out_count(m_h, in.size(), &n) != FDSP_OK) return false;
-        out.resize(n);
-        uint64_t got = 0;
-        if (fdsp_fm_demod_apply_host(m_h, gb300_detail::cf(in), in.size(), out.data(), n, &got, nullptr) !=
-            FDSP_OK) {
-            out.clear();
-            return false;
-        }
-        out.resize(got);
-        return !out.empty();
-    }
-
-private:
-    fdsp_fm_demod* m_h = nullptr;
 };
 
 }  // namespace falcon_dsp

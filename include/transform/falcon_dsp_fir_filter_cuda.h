@@ -1,10 +1,10 @@
 /*
  * Drop-in for libfalcon_dsp's falcon_dsp_fir_filter_cuda
  * (hdr/transform/falcon_dsp_fir_filter_cuda.h:113-138) and the free
- * fir_filter_cuda functions (:87-91): y[n] = sum_k h[k] x[n-k] with complex
- * taps, history carried across applies, output length = input length.  The
- * int16 overload converts in and truncates out like
- * src/transform/falcon_dsp_fir_filter.cc:151-175.
+ * fir_filter_cuda functions (:87-91).  As in the reference it derives from
+ * falcon_dsp_fir_filter (falcon_dsp_fir_filter.h here, GPU-backed too) and
+ * overrides both applies, so it can be used through a base-class reference
+ * or pointer.
  */
 #ifndef FALCON_DSP_FIR_FILTER_CUDA_H
 #define FALCON_DSP_FIR_FILTER_CUDA_H
@@ -13,50 +13,24 @@
 #include <cstdint>
 #include <vector>
 
-#include "falcon_dsp_gb300_detail.h"
+#include "falcon_dsp_fir_filter.h"
 
 namespace falcon_dsp {
 
-class falcon_dsp_fir_filter_cuda {
+class falcon_dsp_fir_filter_cuda : public falcon_dsp_fir_filter {
 public:
-    /* The reference constructs from the taps; a failed set-up leaves the
-     * object unusable and every apply returns false. */
-    explicit falcon_dsp_fir_filter_cuda(std::vector<std::complex<float>>& coeffs) {
-        if (coeffs.empty() ||
-            fdsp_fir_create(gb300_detail::cf(coeffs), (uint32_t)coeffs.size(), &m_h) != FDSP_OK)
-            m_h = nullptr;
-    }
-    virtual ~falcon_dsp_fir_filter_cuda(void) {
-        if (m_h) fdsp_fir_destroy(m_h);
-    }
+    explicit falcon_dsp_fir_filter_cuda(std::vector<std::complex<float>>& coeffs) : falcon_dsp_fir_filter(coeffs) {}
+    ~falcon_dsp_fir_filter_cuda(void) override = default;
     falcon_dsp_fir_filter_cuda(void) = delete;
     falcon_dsp_fir_filter_cuda(const falcon_dsp_fir_filter_cuda&) = delete;
     falcon_dsp_fir_filter_cuda& operator=(const falcon_dsp_fir_filter_cuda&) = delete;
 
-    void reset_state(void) {
-        if (m_h) fdsp_fir_reset(m_h);
+    bool apply(std::vector<std::complex<int16_t>>& in, std::vector<std::complex<int16_t>>& out) override {
+        return falcon_dsp_fir_filter::apply(in, out);
     }
-
-    virtual bool apply(std::vector<std::complex<int16_t>>& in, std::vector<std::complex<int16_t>>& out) {
-        std::vector<std::complex<float>> tin = gb300_detail::to_float(in), tout;
-        const bool ok = apply(tin, tout);
-        gb300_detail::to_int16(tout, out);
-        return ok;
+    bool apply(std::vector<std::complex<float>>& in, std::vector<std::complex<float>>& out) override {
+        return falcon_dsp_fir_filter::apply(in, out);
     }
-
-    virtual bool apply(std::vector<std::complex<float>>& in, std::vector<std::complex<float>>& out) {
-        out.clear();
-        if (!m_h || in.empty()) return false;
-        out.resize(in.size());
-        if (fdsp_fir_apply_host(m_h, gb300_detail::cf(in), in.size(), gb300_detail::cf(out), nullptr) != FDSP_OK) {
-            out.clear();
-            return false;
-        }
-        return true;
-    }
-
-private:
-    fdsp_fir* m_h = nullptr;
 };
 
 inline bool fir_filter_cuda(std::vector<std::complex<float>>& coeffs, std::vector<std::complex<int16_t>>& in,

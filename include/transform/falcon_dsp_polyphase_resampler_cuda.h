@@ -1,12 +1,10 @@
 /*
  * Drop-in for libfalcon_dsp's falcon_dsp_polyphase_resampler_cuda
- * (hdr/transform/falcon_dsp_polyphase_resampler_cuda.h:187-226) and the
- * CPU class interface it derives from
- * (hdr/transform/falcon_dsp_polyphase_resampler.h:168-195): initialize(up,
- * down, coeffs) once, apply() streams with the CPU loop's carried phase and
- * xOffset, only the real parts of the taps are used, apply() returns the
- * number of outputs (0 when not initialized or on failure, as the CUDA
- * class returns 0 when not initialized).
+ * (hdr/transform/falcon_dsp_polyphase_resampler_cuda.h:187-226).  As in the
+ * reference it derives from falcon_dsp_polyphase_resampler and overrides
+ * initialize/apply, so it can be used through a base-class reference or
+ * pointer.  Both classes run on the GPU (the base class here has no CPU
+ * implementation); see falcon_dsp_polyphase_resampler.h for the semantics.
  */
 #ifndef FALCON_DSP_POLYPHASE_RESAMPLER_CUDA_H
 #define FALCON_DSP_POLYPHASE_RESAMPLER_CUDA_H
@@ -15,72 +13,26 @@
 #include <cstdint>
 #include <vector>
 
-#include "falcon_dsp_gb300_detail.h"
+#include "falcon_dsp_polyphase_resampler.h"
 
 namespace falcon_dsp {
 
-class falcon_dsp_polyphase_resampler_cuda {
+class falcon_dsp_polyphase_resampler_cuda : public falcon_dsp_polyphase_resampler {
 public:
     falcon_dsp_polyphase_resampler_cuda(void) = default;
-    virtual ~falcon_dsp_polyphase_resampler_cuda(void) {
-        if (m_h) fdsp_resampler_destroy(m_h);
-    }
+    ~falcon_dsp_polyphase_resampler_cuda(void) override = default;
     falcon_dsp_polyphase_resampler_cuda(const falcon_dsp_polyphase_resampler_cuda&) = delete;
     falcon_dsp_polyphase_resampler_cuda& operator=(const falcon_dsp_polyphase_resampler_cuda&) = delete;
 
-    virtual bool initialize(uint32_t up_rate, uint32_t down_rate, const std::vector<std::complex<float>>& filter_coeffs) {
-        if (m_h || filter_coeffs.empty()) return false;
-        if (fdsp_resampler_create(up_rate, down_rate, gb300_detail::cf(filter_coeffs), (uint32_t)filter_coeffs.size(),
-                                  &m_h) != FDSP_OK) {
-            m_h = nullptr;
-            return false;
-        }
-        return true;
+    bool initialize(uint32_t up_rate, uint32_t down_rate, const std::vector<std::complex<float>>& filter_coeffs) override {
+        return falcon_dsp_polyphase_resampler::initialize(up_rate, down_rate, filter_coeffs);
     }
-
-    void reset_state(void) {
-        if (m_h) fdsp_resampler_reset(m_h);
+    int32_t apply(std::vector<float>& in, std::vector<float>& out) override {
+        return falcon_dsp_polyphase_resampler::apply(in, out);
     }
-
-    /* Real input: taken as complex with zero imaginary part, real part returned
-     * (src/transform/falcon_dsp_polyphase_resampler.cc:230-253). */
-    virtual int32_t apply(std::vector<float>& in, std::vector<float>& out) {
-        out.clear();
-        std::vector<std::complex<float>> tin(in.begin(), in.end()), tout;
-        const int32_t n = apply(tin, tout);
-        out.reserve(tout.size());
-        for (const auto& s : tout) out.push_back(s.real());
-        return n;
+    int32_t apply(std::vector<std::complex<float>>& in, std::vector<std::complex<float>>& out) override {
+        return falcon_dsp_polyphase_resampler::apply(in, out);
     }
-
-    virtual int32_t apply(std::vector<std::complex<float>>& in, std::vector<std::complex<float>>& out) {
-        out.clear();
-        if (!m_h) return 0;
-        uint64_t cnt = 0, got = 0;
-        if (fdsp_resampler_out_count(m_h, in.size(), &cnt) != FDSP_OK) return 0;
-        out.resize(cnt);
-        if (fdsp_resampler_apply_host(m_h, gb300_detail::cf(in), in.size(), gb300_detail::cf(out), cnt, &got,
-                                      nullptr) != FDSP_OK) {
-            out.clear();
-            return 0;
-        }
-        out.resize(got);
-        return (int32_t)got;
-    }
-
-    /* needed_out_count() exactly as the reference computes it
-     * (src/transform/falcon_dsp_polyphase_resampler.cc:204-228). */
-    uint32_t needed_out_count(uint32_t inCount) {
-        uint32_t n = 0;
-        return (m_h && fdsp_resampler_needed_out_count(m_h, inCount, &n) == FDSP_OK) ? n : 0;
-    }
-    uint32_t coeffs_per_phase(void) {
-        uint32_t n = 0;
-        return (m_h && fdsp_resampler_coeffs_per_phase(m_h, &n) == FDSP_OK) ? n : 0;
-    }
-
-private:
-    fdsp_resampler* m_h = nullptr;
 };
 
 }  // namespace falcon_dsp

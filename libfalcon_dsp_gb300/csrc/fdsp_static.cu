@@ -101,7 +101,8 @@ extern "C" int fdsp_resample_static(uint32_t up_rate, uint32_t down_rate, const 
   st = cuda_status(cudaMemcpyAsync(slot.taps, coeffs, (size_t)num_coeffs * sizeof(float2), cudaMemcpyDefault, s));
   if (st != FDSP_OK) return st;
   if (cnt > 0) {
-    const uint32_t T = (num_coeffs + up_rate - 1) / up_rate;
+    // taps per phase, in 64 bits: up_rate near 2^32 must not wrap the sum
+    const uint32_t T = (uint32_t)(((uint64_t)num_coeffs + up_rate - 1) / up_rate);
     const int64_t blocks = std::min<int64_t>((int64_t)((cnt + 255) / 256), (int64_t)slot.num_sms * 8);
     resample_static_kernel<<<(unsigned)blocks, 256, 0, s>>>(slot.taps, num_coeffs, up_rate, down_rate, T,
                                                             reinterpret_cast<const float2*>(d_in), (int64_t)n_in,

@@ -24,7 +24,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libfdsp_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfdsp_ref.so")
-REF_ROOT_DEFAULT = "/root/reference"
 
 _vp = C.c_void_p
 _u32, _i32, _u64, _i64, _dbl = C.c_uint32, C.c_int32, C.c_uint64, C.c_int64, C.c_double
@@ -33,13 +32,18 @@ _dp = C.POINTER(C.c_double)
 
 
 def build(with_reference: bool | None = None) -> None:
-    """Compile the C restatement and, when the reference checkout is present,
-    the reference's own CPU sources (oracle/_ref)."""
+    """Compile the C restatement and, when FDSP_REF_ROOT names a reference
+    checkout, the reference's own CPU sources (oracle/_ref).  Without
+    FDSP_REF_ROOT the reference build is skipped; the committed fixtures
+    under tests/golden/ (made from that build) still pin the restatement."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref_root = os.environ.get("FDSP_REF_ROOT", REF_ROOT_DEFAULT)
+    ref_root = os.environ.get("FDSP_REF_ROOT")
     if with_reference is None:
-        with_reference = os.path.isdir(os.path.join(ref_root, "src", "transform"))
+        with_reference = bool(ref_root)
     if with_reference:
+        if not ref_root or not os.path.isdir(os.path.join(ref_root, "src", "transform")):
+            raise RuntimeError("FDSP_REF_ROOT must name a libfalcon_dsp checkout (with src/transform) "
+                               "to build the reference's CPU sources")
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={ref_root}"], check=True)
 
 

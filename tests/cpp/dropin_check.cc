@@ -1,12 +1,16 @@
 // Drives the drop-in C++ classes of include/transform the way a libfalcon_dsp
 // caller would, on deterministic inputs, and writes every input and output as
 // raw little-endian arrays into the directory given as argv[1]; the Python
-// test compares them with the oracle.  Exit status 0 when every call
-// succeeded.
+// test compares them with the oracle.  The *_cuda objects are driven through
+// references and pointers to their base classes (falcon_dsp_polyphase_resampler,
+// falcon_dsp_freq_shift, falcon_dsp_fir_filter, falcon_dsp_fm_demodulator),
+// as callers written against the reference's class hierarchy hold them.
+// Exit status 0 when every call succeeded.
 #include <cmath>
 #include <complex>
 #include <cstdint>
 #include <cstdio>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -90,7 +94,8 @@ int main(int argc, char** argv) {
         cvec taps = noise(3528);
         for (auto& t : taps) t = {t.real(), 0.f};
         dump("rs_taps.bin", taps);
-        falcon_dsp_polyphase_resampler_cuda r;
+        falcon_dsp_polyphase_resampler_cuda r_obj;
+        falcon_dsp_polyphase_resampler& r = r_obj;  // virtual dispatch through the base class
         check(r.initialize(147, 160, taps), "resampler initialize");
         check(r.coeffs_per_phase() == 24, "coeffs_per_phase");
         for (int b = 0; b < 2; ++b) {
@@ -100,11 +105,11 @@ int main(int argc, char** argv) {
             dump("rs_in" + std::to_string(b) + ".bin", in);
             dump("rs_out" + std::to_string(b) + ".bin", out);
         }
-        falcon_dsp_polyphase_resampler_cuda rr;
-        check(rr.initialize(2, 3, taps), "real resampler initialize");
+        std::unique_ptr<falcon_dsp_polyphase_resampler> rr(new falcon_dsp_polyphase_resampler_cuda());
+        check(rr->initialize(2, 3, taps), "real resampler initialize");
         std::vector<float> rin(1000), rout;
         for (auto& s : rin) s = rnd();
-        check(rr.apply(rin, rout) > 0, "real resampler apply");
+        check(rr->apply(rin, rout) > 0, "real resampler apply");
         dump("rsr_in.bin", rin);
         dump("rsr_out.bin", rout);
     }
@@ -119,7 +124,8 @@ int main(int argc, char** argv) {
         dump("fs_in.bin", in);
         dump("fs_out0.bin", out[0]);
         dump("fs_out1.bin", out[1]);
-        falcon_dsp_freq_shift_cuda s16;
+        falcon_dsp_freq_shift_cuda s16_obj;
+        falcon_dsp_freq_shift& s16 = s16_obj;
         check(s16.initialize(1000000, 123456), "int16 freq shift initialize");
         std::vector<std::complex<int16_t>> i16(500), o16;
         for (auto& v : i16) v = {(int16_t)(rnd() * 3000), (int16_t)(rnd() * 3000)};
@@ -131,7 +137,8 @@ int main(int argc, char** argv) {
     {
         cvec taps = noise(129);
         dump("fir_taps.bin", taps);
-        falcon_dsp_fir_filter_cuda f(taps);
+        falcon_dsp_fir_filter_cuda f_obj(taps);
+        falcon_dsp_fir_filter& f = f_obj;
         for (int b = 0; b < 2; ++b) {
             cvec in = noise(2000 + 50 * b), out;
             check(f.apply(in, out) && out.size() == in.size(), "fir apply");
@@ -139,7 +146,8 @@ int main(int argc, char** argv) {
             dump("fir_out" + std::to_string(b) + ".bin", out);
         }
         cvec t3 = {{0.5f, 0.f}, {2.f, 0.f}, {4.f, 0.f}};
-        falcon_dsp_fir_filter_cuda f16(t3);
+        std::unique_ptr<falcon_dsp_fir_filter> f16p(new falcon_dsp_fir_filter_cuda(t3));
+        falcon_dsp_fir_filter& f16 = *f16p;
         std::vector<std::complex<int16_t>> i16(64), o16;
         for (size_t k = 0; k < i16.size(); ++k) i16[k] = {(int16_t)(k * 7 % 101 - 50), (int16_t)(k * 3 % 53 - 26)};
         check(f16.apply(i16, o16) && o16.size() == i16.size(), "int16 fir apply");
@@ -182,7 +190,8 @@ int main(int argc, char** argv) {
     }
     // FM demodulator: station at -150 kHz in a 1.14 MS/s capture
     {
-        falcon_dsp_fm_demodulator_cuda fm;
+        falcon_dsp_fm_demodulator_cuda fm_obj;
+        falcon_dsp_fm_demodulator& fm = fm_obj;
         check(!fm.initialize(1140000, 150000, 60e-6f), "fm bad time constant");
         check(fm.initialize(1140000, 150000), "fm initialize");
         check(!fm.initialize(1140000, 150000), "fm initialize once");

@@ -4,8 +4,11 @@ state): same output count, outputs equal within FP32 rounding.
 
 Two calls in a row with different configurations share the fixed tap array;
 the second has fewer taps than the first, so stale taps left in the array by
-the first call would show up in its outputs.  The file name sorts last so the
-test also runs after every other GPU test of the suite.
+the first call would show up in its outputs.  One case has more phases than
+taps (up > num_coeffs), so most phases read only the zero padding.  After a
+warm-up call, further calls leave the device's free memory unchanged: the
+entry point allocates nothing.  The file name sorts last so the test also
+runs after every other GPU test of the suite.
 """
 import numpy as np
 import pytest
@@ -20,6 +23,7 @@ CASES = [
     (3, 2, 401, 50_000, 1),
     (2, 5, 23, 40_001, 2),
     (1, 8, 2048, 65_536, 3),
+    (7, 3, 5, 30_000, 4),  # up > num_coeffs: phases 5 and 6 hold only padding
 ]
 
 
@@ -63,3 +67,33 @@ def test_static_rejects_oversized_taps_and_small_output():
     got = F.resample_static(2, 1, h, x, out)
     torch.cuda.synchronize()
     assert rel_rms(got.cpu().numpy(), ref.cpu().numpy()) <= 1e-5
+
+
+def test_static_allocates_nothing_after_warmup():
+    torch = pytest.importorskip("torch")
+    x = _signal(200_000, 7, torch)
+    out = torch.empty(800_000, dtype=torch.complex64, device="cuda")
+    h = _taps(1024, 7)
+    F.resample_static(3, 1, h, x, out)  # warm-up: first-call set-up of the device
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for up, down, nt in ((3, 1, 1024), (2, 7, 8000), (5, 4, 3)):
+        F.resample_static(up, down, _taps(nt, up), x, out)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+
+
+def test_static_up_rate_near_2_32_keeps_one_tap_per_phase():
+    # taps per phase = ceil(16 / (2^32 - 1)) = 1: computed without wrapping,
+    # so y[m] = Re(h[0]) x[m] for up = down
+    torch = pytest.importorskip("torch")
+    x = _signal(4096, 8, torch)
+    out = torch.empty(4096, dtype=torch.complex64, device="cuda")
+    h = _taps(16, 8)
+    big = (1 << 32) - 1
+    got = F.resample_static(big, big, h, x, out)
+    torch.cuda.synchronize()
+    assert got.numel() == 4096
+    want = x.cpu().numpy() * np.float32(h[0].real)
+    assert rel_rms(got.cpu().numpy(), want) <= 1e-6
