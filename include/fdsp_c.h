@@ -51,7 +51,9 @@ enum fdsp_status {
     FDSP_ERR_CAPACITY = -5,        /* an output buffer is smaller than the output count */
     FDSP_ERR_UNSUPPORTED = -6,     /* configuration outside this build's limits */
     FDSP_ERR_NO_DEVICE = -7,       /* no CUDA device is visible */
-    FDSP_ERR_NOT_FOUND = -8        /* no predefined filter for the requested key */
+    FDSP_ERR_NOT_FOUND = -8,       /* no predefined filter for the requested key */
+    FDSP_ERR_TIMEOUT = -9          /* a tensor-core kernel's bounded wait gave up: the outputs of the
+                                      applies since the last status check are incomplete */
 };
 
 /* Short text for a status code (static storage). */
@@ -178,9 +180,24 @@ int fdsp_channelizer_out_count(const fdsp_channelizer *h, uint64_t n_in, uint64_
  * NULL to skip the check) receives n_out[c] samples. */
 int fdsp_channelizer_apply(fdsp_channelizer *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 *const *d_out,
                            const uint64_t *out_cap, uint64_t *n_out, fdsp_stream_t stream);
-/* Select the arithmetic of later applies (fdsp_precision).  Channels whose
- * taps per phase exceed 64 keep the FP32 form in the tensor-core modes. */
+/* Select the arithmetic of later applies (fdsp_precision).  Under a
+ * tensor-core precision every decimation group runs in one persistent
+ * tensor-core launch (any taps per phase); groups beyond that launch's record
+ * limits keep the FP32 form. */
 int fdsp_channelizer_set_precision(fdsp_channelizer *h, int precision);
+/* Error status of the applies enqueued so far (no counterpart in the
+ * reference, whose CUDA errors exit the process,
+ * src/utilities/falcon_dsp_cuda_utils.cu:84-94): synchronises `stream`, then
+ * returns FDSP_ERR_TIMEOUT when a tensor-core kernel's bounded wait gave up
+ * since the last check (and clears that record), a CUDA error as
+ * FDSP_ERR_CUDA, else FDSP_OK.  The *_apply_host entry points check it
+ * themselves before returning. */
+int fdsp_channelizer_status(fdsp_channelizer *h, fdsp_stream_t stream);
+/* Bounded waits of the tensor-core kernel: a wait gives up after max_polls
+ * polls (each suspends the waiting thread for up to ~2 us; default 2^20).
+ * withhold_copies != 0 makes later launches issue no operand copies, so every
+ * wait runs out: a test hook for the timeout path, never for production. */
+int fdsp_channelizer_set_tc_wait(fdsp_channelizer *h, uint32_t max_polls, int withhold_copies);
 /* Kernel launches the most recent apply enqueued (diagnostics, profiling). */
 int fdsp_channelizer_kernel_launches(const fdsp_channelizer *h, uint32_t *n);
 /* Decimation groups that the most recent apply computed on the tensor-core
@@ -190,10 +207,9 @@ int fdsp_channelizer_kernel_launches(const fdsp_channelizer *h, uint32_t *n);
 int fdsp_channelizer_tc_groups(const fdsp_channelizer *h, uint32_t *n);
 /* Autotuner (no counterpart in the reference): times every decimation group
  * (channels sharing a down rate) on an n_in-sample block on `stream` and keeps,
- * per group, the fastest FP32 tile height and, under a tensor-core precision,
- * the faster of the tensor-core and FP32 forms.  It allocates scratch for the
- * trial, synchronises the stream and resets the streaming state; call it after
- * fdsp_channelizer_set_precision and before the first apply. */
+ * per group, the fastest FP32 tile height.  It allocates scratch for the
+ * trial, synchronises the stream and resets the streaming state; call it
+ * before the first apply. */
 int fdsp_channelizer_autotune(fdsp_channelizer *h, uint64_t n_in, fdsp_stream_t stream);
 /* Decimation groups of the channelizer and, per group, its down rate, FP32
  * tile height (output rows per CTA) and whether applies ask for the
@@ -209,13 +225,15 @@ int fdsp_channelizer_set_graph(fdsp_channelizer *h, int enable);
 int fdsp_channelizer_graph_replays(const fdsp_channelizer *h, uint32_t *replays);
 int fdsp_channelizer_group_info(const fdsp_channelizer *h, uint32_t group, uint32_t *down_rate, uint32_t *tile_rows,
                                 int *tensor_core);
-/* Row split S of a group's last tensor-core launch (1 = none; its limit is
- * autotuned among 1, 2, 4): rows j = S i + b run as S work sets at stride
- * S x down_rate, so one staged tile feeds S times the channel columns. */
+/* Row split S of a group's last tensor-core launch (1 = none): rows
+ * j = S i + b run as S output streams whose rows are S x down_rate apart, so
+ * one tile of input rows feeds S times the channel columns (odd down rates
+ * always split by 2 or more: the input rows of a tile must start 16 bytes
+ * apart). */
 int fdsp_channelizer_group_tc_split(const fdsp_channelizer *h, uint32_t group, uint32_t *split);
-/* Largest row split (1..8) of every group's tensor-core form until the next
- * autotune; the split used is the largest one up to it whose columns
- * (<= 128) and merged window (<= 128 taps) fit one product. */
+/* Largest row split (1..32, default 32) of every group's tensor-core form;
+ * the split used is the largest power of two up to it whose streams still
+ * fit one 32-stream product and whose windows grow by at most a quarter. */
 int fdsp_channelizer_set_tc_split(fdsp_channelizer *h, uint32_t max_split);
 /* apply(in, out) on host buffers (copies in, computes, copies out, syncs). */
 int fdsp_channelizer_apply_host(fdsp_channelizer *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *const *h_out,
@@ -261,6 +279,14 @@ int fdsp_resampler_apply_host(fdsp_resampler *h, const fdsp_cf32 *h_in, uint64_t
 /* complex int16 input (see fdsp_channelizer_apply_ci16), complex64 output */
 int fdsp_resampler_apply_ci16(fdsp_resampler *h, const int16_t *d_in, uint64_t n_in, fdsp_cf32 *d_out,
                               uint64_t out_cap, uint64_t *n_out, fdsp_stream_t stream);
+/* Arithmetic of later applies (fdsp_precision; no counterpart in the
+ * reference): the tensor-core forms run the filter as one persistent
+ * tcgen05 launch for any taps per phase, e.g. a long FIR followed by a
+ * decimation (up = 1).  1 in *n when the last apply ran on the tensor cores.
+ * fdsp_resampler_status: as fdsp_channelizer_status. */
+int fdsp_resampler_set_precision(fdsp_resampler *h, int precision);
+int fdsp_resampler_tc_groups(const fdsp_resampler *h, uint32_t *n);
+int fdsp_resampler_status(fdsp_resampler *h, fdsp_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * One-shot polyphase resampling that allocates nothing.
@@ -338,11 +364,13 @@ int fdsp_fir_apply(fdsp_fir *h, const fdsp_cf32 *d_in, uint64_t n_in, fdsp_cf32 
 int fdsp_fir_apply_host(fdsp_fir *h, const fdsp_cf32 *h_in, uint64_t n_in, fdsp_cf32 *h_out, fdsp_stream_t stream);
 /* FDSP_PRECISION_FP32 (default) or the tensor-core split-precision forms
  * FDSP_PRECISION_FP16X3 / FDSP_PRECISION_BF16X3: the FIR as a Toeplitz
- * product on tcgen05 (32 consecutive outputs per row of the tile), for up to
- * 64 taps (longer filters keep the FP32 kernel).  Resets the streaming state. */
+ * product on tcgen05 (32 consecutive outputs per row of a tile: 32 output
+ * streams whose windows start one sample apart), any number of taps. */
 int fdsp_fir_set_precision(fdsp_fir *h, int precision);
 /* 1 when the last apply ran on the tensor-core kernel, else 0 */
 int fdsp_fir_tc_groups(const fdsp_fir *h, uint32_t *n);
+/* as fdsp_channelizer_status */
+int fdsp_fir_status(fdsp_fir *h, fdsp_stream_t stream);
 /* int16 overload (src/transform/falcon_dsp_fir_filter.cc:151-175): complex
  * int16 in (converted inside the filter kernel), complex int16 out
  * (truncated toward zero). */

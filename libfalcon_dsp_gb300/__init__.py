@@ -206,10 +206,22 @@ class MultiRateChannelizerCuda(_Handle):
         _capi.call("fdsp_channelizer_set_precision", self._h, self.PRECISION[mode])
 
     def set_tc_split(self, max_split: int) -> None:
-        """Largest row split (1..8) of the tensor-core form: a group's rows
-        j = S i + b run as S work sets at stride S x down_rate, so one staged
-        tile feeds S times the channel columns.  autotune() sets it per group."""
+        """Largest row split (1..32, default 32) of the tensor-core form: a
+        group's rows j = S i + b run as S output streams whose rows are
+        S x down_rate apart, so one tile of input rows feeds S times the
+        channel columns."""
         _capi.call("fdsp_channelizer_set_tc_split", self._h, int(max_split))
+
+    def status(self, stream: int | None = None) -> None:
+        """Synchronise `stream` and raise FdspError (FDSP_ERR_TIMEOUT) when a
+        tensor-core kernel's bounded wait gave up since the last check."""
+        s = _stream_handle() if stream is None else stream
+        _capi.call("fdsp_channelizer_status", self._h, C.c_void_p(s))
+
+    def set_tc_wait(self, max_polls: int = 1 << 20, withhold_copies: bool = False) -> None:
+        """Polls before a tensor-core wait gives up; withhold_copies is a test
+        hook that makes every wait run out."""
+        _capi.call("fdsp_channelizer_set_tc_wait", self._h, int(max_polls), 1 if withhold_copies else 0)
 
     def kernel_launches(self) -> int:
         v = C.c_uint32()
@@ -218,8 +230,8 @@ class MultiRateChannelizerCuda(_Handle):
 
     def autotune(self, n_in: int, stream: int | None = None) -> list[dict]:
         """Time each decimation group on an n_in-sample block and keep the
-        fastest FP32 tile height and (tensor-core precisions) the faster
-        form per group; resets the streaming state.  Returns group_info()."""
+        fastest FP32 tile height per group; resets the streaming state.
+        Returns group_info()."""
         s = _stream_handle() if stream is None else stream
         _capi.call("fdsp_channelizer_autotune", self._h, int(n_in), C.c_void_p(s))
         return self.group_info()
@@ -364,6 +376,20 @@ class PolyphaseResamplerCuda(_Handle):
         _capi.call("fdsp_resampler_state", self._h, C.byref(ph), C.byref(xo))
         return ph.value, xo.value
 
+    def set_precision(self, mode: str = "fp32") -> None:
+        """'fp32' (default), or the tensor-core forms 'fp16x3' / 'bf16x3'."""
+        _capi.call("fdsp_resampler_set_precision", self._h, MultiRateChannelizerCuda.PRECISION[mode])
+
+    def tc_groups(self) -> int:
+        """1 when the last apply ran on the tensor-core kernel."""
+        v = C.c_uint32()
+        _capi.call("fdsp_resampler_tc_groups", self._h, C.byref(v))
+        return v.value
+
+    def status(self, stream: int | None = None) -> None:
+        s = _stream_handle() if stream is None else stream
+        _capi.call("fdsp_resampler_status", self._h, C.c_void_p(s))
+
     def apply(self, x, out=None, stream: int | None = None):
         if _is_tensor(x):
             torch = _torch()
@@ -476,9 +502,13 @@ class FirFilterCuda(_Handle):
 
     def set_precision(self, mode: str = "fp32") -> None:
         """'fp32' (default) or the tensor-core forms 'fp16x3' / 'bf16x3'
-        (Toeplitz product, (hi+lo)(hi+lo), FP32 accumulation; up to 64 taps).
-        Resets the streaming state."""
+        (Toeplitz product, (hi+lo)(hi+lo), FP32 accumulation; any number of
+        taps).  The streaming state carries over."""
         _capi.call("fdsp_fir_set_precision", self._h, MultiRateChannelizerCuda.PRECISION[mode])
+
+    def status(self, stream: int | None = None) -> None:
+        s = _stream_handle() if stream is None else stream
+        _capi.call("fdsp_fir_status", self._h, C.c_void_p(s))
 
     def tc_groups(self) -> int:
         v = C.c_uint32()

@@ -23,8 +23,10 @@ STATUS = {
     -6: "FDSP_ERR_UNSUPPORTED",
     -7: "FDSP_ERR_NO_DEVICE",
     -8: "FDSP_ERR_NOT_FOUND",
+    -9: "FDSP_ERR_TIMEOUT",
 }
 FDSP_ERR_NOT_FOUND = -8
+FDSP_ERR_TIMEOUT = -9
 
 
 class cf32(C.Structure):
@@ -85,6 +87,12 @@ SIGNATURES = {
     "fdsp_fir_tc_groups": [_vp, _pu32],
     "fdsp_fir_apply_ci16_host": [_vp, _vp, _u64, _vp, _vp],
     "fdsp_channelizer_tc_groups": [_vp, _pu32],
+    "fdsp_channelizer_status": [_vp, _vp],
+    "fdsp_channelizer_set_tc_wait": [_vp, _u32, C.c_int],
+    "fdsp_resampler_set_precision": [_vp, C.c_int],
+    "fdsp_resampler_tc_groups": [_vp, _pu32],
+    "fdsp_resampler_status": [_vp, _vp],
+    "fdsp_fir_status": [_vp, _vp],
     "fdsp_server_create": [_u64, _u32, _pp],
     "fdsp_server_destroy": [_vp],
     "fdsp_server_open": [_vp, _u32, _vp, _u32, _u64, C.c_int, _pu32],

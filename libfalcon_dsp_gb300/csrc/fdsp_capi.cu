@@ -42,11 +42,9 @@ struct fdsp_resampler {
 };
 
 struct fdsp_fir {
-  PolyEngine eng;                   // y[n] = sum_k h[k] x[n-k]: one channel, up = down = 1
-  std::unique_ptr<PolyEngine> toe;  // tensor-core precisions: the Toeplitz form below
-  std::vector<fdsp_cf32> taps;
+  PolyEngine eng;  // y[n] = sum_k h[k] x[n-k]: one channel, up = down = 1
   DevBuf in, out;
-  PolyEngine& active() { return toe ? *toe : eng; }
+  PolyEngine& active() { return eng; }
 };
 
 struct fdsp_freq_shift {
@@ -70,6 +68,14 @@ struct fdsp_polar {
   }
 };
 
+// Status of the applies enqueued on `stream` so far: CUDA errors, then the
+// tensor-core kernel's bounded-wait record (cleared by the read).
+static int engine_status(PolyEngine& e, cudaStream_t s) {
+  const int st = cuda_status(cudaStreamSynchronize(s));
+  if (st != FDSP_OK) return st;
+  return e.tc_error() ? FDSP_ERR_TIMEOUT : FDSP_OK;
+}
+
 extern "C" {
 
 const char* fdsp_status_string(int status) {
@@ -83,6 +89,7 @@ const char* fdsp_status_string(int status) {
     case FDSP_ERR_UNSUPPORTED: return "configuration outside this build's limits";
     case FDSP_ERR_NO_DEVICE: return "no CUDA device";
     case FDSP_ERR_NOT_FOUND: return "no predefined filter for this key";
+    case FDSP_ERR_TIMEOUT: return "a tensor-core kernel's bounded wait gave up (outputs incomplete)";
     default: return "unknown status";
   }
 }
@@ -208,6 +215,18 @@ int fdsp_channelizer_apply(fdsp_channelizer* h, const fdsp_cf32* d_in, uint64_t 
                       n_out, (cudaStream_t)stream);
 }
 
+int fdsp_channelizer_status(fdsp_channelizer* h, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return engine_status(h->eng, (cudaStream_t)stream);
+}
+
+int fdsp_channelizer_set_tc_wait(fdsp_channelizer* h, uint32_t max_polls, int withhold_copies) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (max_polls == 0) return FDSP_ERR_INVALID_ARG;
+  h->eng.set_tc_wait(max_polls, withhold_copies != 0 ? 1 : 0);
+  return FDSP_OK;
+}
+
 int fdsp_channelizer_apply_ci16(fdsp_channelizer* h, const int16_t* d_in, uint64_t n_in, fdsp_cf32* const* d_out,
                                 const uint64_t* out_cap, uint64_t* n_out, fdsp_stream_t stream) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
@@ -305,7 +324,7 @@ int fdsp_channelizer_apply_host(fdsp_channelizer* h, const fdsp_cf32* h_in, uint
       FDSP_TRY(cuda_status(
           cudaMemcpyAsync(h_out[c], dptr[c], n_out[c] * sizeof(float2), cudaMemcpyDeviceToHost, s)));
   }
-  return cuda_status(cudaStreamSynchronize(s));
+  return engine_status(h->eng, s);
 }
 
 int fdsp_channelizer_apply_ci16_host(fdsp_channelizer* h, const int16_t* h_in, uint64_t n_in, fdsp_cf32* const* h_out,
@@ -334,7 +353,7 @@ int fdsp_channelizer_apply_ci16_host(fdsp_channelizer* h, const int16_t* h_in, u
       FDSP_TRY(cuda_status(
           cudaMemcpyAsync(h_out[c], dptr[c], n_out[c] * sizeof(float2), cudaMemcpyDeviceToHost, s)));
   }
-  return cuda_status(cudaStreamSynchronize(s));
+  return engine_status(h->eng, s);
 }
 
 /* ---------------- resampler ---------------- */
@@ -437,7 +456,24 @@ int fdsp_resampler_apply_host(fdsp_resampler* h, const fdsp_cf32* h_in, uint64_t
   FDSP_TRY(h->eng.apply(static_cast<const float2*>(h->in.p), n_in, &o, nullptr, n_out, s));
   if (*n_out)
     FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out, o, *n_out * sizeof(float2), cudaMemcpyDeviceToHost, s)));
-  return cuda_status(cudaStreamSynchronize(s));
+  return engine_status(h->eng, s);
+}
+
+int fdsp_resampler_set_precision(fdsp_resampler* h, int precision) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return h->eng.set_precision(precision);
+}
+
+int fdsp_resampler_tc_groups(const fdsp_resampler* h, uint32_t* n) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  if (!n) return FDSP_ERR_INVALID_ARG;
+  *n = (uint32_t)h->eng.tc_groups_last();
+  return FDSP_OK;
+}
+
+int fdsp_resampler_status(fdsp_resampler* h, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return engine_status(h->eng, (cudaStream_t)stream);
 }
 
 /* ---------------- FIR ---------------- */
@@ -459,51 +495,30 @@ int fdsp_fir_create(const fdsp_cf32* coeffs, uint32_t ncoeffs, fdsp_fir** out) {
     delete h;
     return st;
   }
-  h->taps.assign(coeffs, coeffs + ncoeffs);
   *out = h;
   return FDSP_OK;
 }
 
-// Tensor-core FIR.  The filter equals a resampler with up = down = L and the
-// taps spread L apart (h[k] at k L, zeros between): every output then uses
-// tap phase 0, and the engine splits the outputs into L interleaved lanes
-// (output m = r + L j, r < L) that read the input r samples apart.  On the
-// tensor-core kernel those L lanes are the columns of one merge set: a
-// Toeplitz product, with the input tile read once for L outputs a row.
-constexpr uint32_t kFirToeplitzLanes = 32;
-
+// Tensor-core FIR: the one-channel engine under a tensor-core precision.
+// The planner splits its outputs into 32 interleaved streams (output
+// m = b + 32 i, windows starting b samples apart), the 32 output streams of
+// one product: a Toeplitz matrix product that reads each input row once for
+// 32 outputs.
 int fdsp_fir_set_precision(fdsp_fir* h, int precision) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
-  if (precision == FDSP_PRECISION_FP32) {
-    h->toe.reset();
-    h->eng.reset();
-    return FDSP_OK;
-  }
-  if (precision != FDSP_PRECISION_FP16X3 && precision != FDSP_PRECISION_BF16X3) return FDSP_ERR_INVALID_ARG;
-  const uint32_t L = kFirToeplitzLanes;
-  std::vector<fdsp_cf32> spread((size_t)h->taps.size() * L, fdsp_cf32{0.f, 0.f});
-  for (size_t k = 0; k < h->taps.size(); ++k) spread[k * L] = h->taps[k];
-  std::unique_ptr<PolyEngine> e(new (std::nothrow) PolyEngine());
-  if (!e) return FDSP_ERR_ALLOC;
-  fdsp_channel_cfg c;
-  c.output_sample_rate_in_sps = 0;
-  c.freq_shift_in_hz = 0;
-  c.up_rate = L;
-  c.down_rate = L;
-  c.resample_filter_coeffs = spread.data();
-  c.num_coeffs = (uint32_t)spread.size();
-  FDSP_TRY(e->init(1, &c, 1, true));
-  FDSP_TRY(e->set_precision(precision));
-  h->toe = std::move(e);
-  h->eng.reset();
-  return FDSP_OK;
+  return h->eng.set_precision(precision);
 }
 
 int fdsp_fir_tc_groups(const fdsp_fir* h, uint32_t* n) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
   if (!n) return FDSP_ERR_INVALID_ARG;
-  *n = h->toe ? (uint32_t)h->toe->tc_groups_last() : 0u;
+  *n = (uint32_t)h->eng.tc_groups_last();
   return FDSP_OK;
+}
+
+int fdsp_fir_status(fdsp_fir* h, fdsp_stream_t stream) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return engine_status(h->eng, (cudaStream_t)stream);
 }
 
 int fdsp_fir_destroy(fdsp_fir* h) {
@@ -536,7 +551,7 @@ int fdsp_fir_apply_host(fdsp_fir* h, const fdsp_cf32* h_in, uint64_t n_in, fdsp_
   uint64_t cnt = 0;
   FDSP_TRY(h->active().apply(static_cast<const float2*>(h->in.p), n_in, &o, nullptr, &cnt, s));
   if (cnt) FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out, o, cnt * sizeof(float2), cudaMemcpyDeviceToHost, s)));
-  return cuda_status(cudaStreamSynchronize(s));
+  return engine_status(h->eng, s);
 }
 
 int fdsp_fir_apply_ci16(fdsp_fir* h, const int16_t* d_in, uint64_t n_in, int16_t* d_out, fdsp_stream_t stream) {
@@ -561,7 +576,7 @@ int fdsp_fir_apply_ci16_host(fdsp_fir* h, const int16_t* h_in, uint64_t n_in, in
   FDSP_TRY(cuda_status(cudaMemcpyAsync(din, h_in, n_in * 2 * sizeof(int16_t), cudaMemcpyHostToDevice, s)));
   FDSP_TRY(fdsp_fir_apply_ci16(h, din, n_in, dout, stream));
   FDSP_TRY(cuda_status(cudaMemcpyAsync(h_out, dout, n_in * 2 * sizeof(int16_t), cudaMemcpyDeviceToHost, s)));
-  return cuda_status(cudaStreamSynchronize(s));
+  return engine_status(h->eng, s);
 }
 
 /* ---------------- frequency shift ---------------- */

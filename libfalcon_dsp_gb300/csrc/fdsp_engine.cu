@@ -715,7 +715,7 @@ void PolyEngine::set_graph(bool on) {
 }
 
 bool PolyEngine::use_tc_for(int eg) const {
-  if (precision_ == FDSP_PRECISION_FP32 || force_ == 0 || !group_tc_ok(eg)) return false;
+  if (precision_ == FDSP_PRECISION_FP32 || force_ == 0) return false;
   return force_ == 1 || groups_[eg].use_tc != 0;
 }
 
@@ -732,7 +732,6 @@ int PolyEngine::autotune(uint64_t n, cudaStream_t stream) {
   }
   prof_ev_.assign(2 * ng, nullptr);
   prof_hit_.assign(ng, 0);
-  prof_tc_.assign(ng, 0);
   for (size_t i = 0; i < prof_ev_.size() && st == FDSP_OK; ++i) st = cuda_status(cudaEventCreate(&prof_ev_[i]));
   std::vector<uint64_t> counts(chans_.size());
   // minimum over 3 timed applies (after one untimed) of each group's time
@@ -778,28 +777,6 @@ int PolyEngine::autotune(uint64_t n, cudaStream_t stream) {
       }
   }
   for (size_t g = 0; g < ng; ++g) groups_[g].Qt = best_qt[g];
-  if (st == FDSP_OK && precision_ != FDSP_PRECISION_FP32) {
-    // tensor-core form with row splits of up to 1, 2 and 4 (groups with few
-    // channel columns); a group keeps the tensor-core form only where that
-    // kernel really ran (configurations beyond its limits fall back to FP32)
-    // and was faster
-    std::vector<int> best_split(ng, 1), use(ng, 0);
-    const int splits[3] = {1, 2, 4};
-    for (int si = 0; si < 3 && st == FDSP_OK; ++si) {
-      for (size_t g = 0; g < ng; ++g) groups_[g].tc_split = splits[si];
-      st = run(1, t);
-      for (size_t g = 0; g < ng && st == FDSP_OK; ++g)
-        if (prof_tc_[g] && t[g] < best[g]) {
-          best[g] = t[g];
-          best_split[g] = splits[si];
-          use[g] = 1;
-        }
-    }
-    for (size_t g = 0; g < ng; ++g) {
-      groups_[g].use_tc = use[g];
-      groups_[g].tc_split = best_split[g];
-    }
-  }
   force_ = -1;
   for (auto ev : prof_ev_)
     if (ev) cudaEventDestroy(ev);
@@ -923,32 +900,43 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
   L.ngroups = ng;
   L.max_tiles = max_tiles;
   L.nws = nws;
-  // tensor-core groups read the input pre-split into {hi, lo} pairs
-  if (precision_ != FDSP_PRECISION_FP32) {
-    bool any_tc = false;
-    for (int gi = 0; gi < ng; ++gi) any_tc = any_tc || use_tc_for(group_of_d_[L.groups[gi].D]);
-    if (any_tc) {
-      const int st = prepare_tc_input(d_in, n, stream);
-      if (st != FDSP_OK) return st;
+  if (num_sms_ == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev);
+    if (num_sms_ <= 0) num_sms_ = 1;
+  }
+  // tensor-core groups: one prep launch and one filter-bank launch for all of
+  // them; groups the tensor-core plan cannot hold stay on the FP32 kernel
+  std::vector<char> on_tc(ng, 0);
+  {
+    std::vector<int> tcg, fallback;
+    for (int gi = 0; gi < ng; ++gi) {
+      const int eg = group_of_d_[L.groups[gi].D];
+      if (L.groups[gi].ntiles > 0 && use_tc_for(eg)) tcg.push_back(eg);
+    }
+    if (!tcg.empty()) {
+      FDSP_TRY(launch_tc(d_in, n, out, tcg, fallback, stream));
+      for (int gi = 0; gi < ng; ++gi) {
+        const int eg = group_of_d_[L.groups[gi].D];
+        on_tc[gi] = std::find(tcg.begin(), tcg.end(), eg) != tcg.end() &&
+                    std::find(fallback.begin(), fallback.end(), eg) == fallback.end();
+      }
     }
   }
-  // small blocks: the FP32 groups in at most two launches (one per way of
-  // staging taps; grid = tiles x groups, shared memory of the largest group
-  // of the launch); the per-launch cost then stops dominating short blocks
+  // small blocks: the FP32 groups in at most four launches (by way of
+  // staging taps and tile form; grid = tiles x groups, shared memory of the
+  // largest group of the launch); the per-launch cost then stops dominating
+  // short blocks
   {
-    bool fuse = ng > 1 && prof_ev_.empty();
+    int nfp = 0;
     int64_t tiles = 0;
-    for (int gi = 0; gi < ng && fuse; ++gi) {
-      fuse = !use_tc_for(group_of_d_[L.groups[gi].D]);
+    for (int gi = 0; gi < ng; ++gi) {
+      if (on_tc[gi] || L.groups[gi].ntiles <= 0) continue;
+      ++nfp;
       tiles += L.groups[gi].ntiles;
     }
-    if (num_sms_ == 0) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev);
-      if (num_sms_ <= 0) num_sms_ = 1;
-    }
-    if (fuse && tiles <= 3LL * num_sms_ && L.max_tiles > 0) {
+    if (nfp > 1 && prof_ev_.empty() && tiles <= 3LL * num_sms_) {
       int nm = 0;
       for (int pass = 0; pass < 4; ++pass) {  // (taps in shared memory?, sliding window?)
         const int first = nm;
@@ -957,7 +945,7 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
         const int want_smem = (pass & 1) == 0 ? 1 : 0, want_win = pass >> 1;
         for (int gi = 0; gi < ng; ++gi) {
           const GroupDesc& gd = L.groups[gi];
-          if (gd.taps_smem != want_smem || gd.win != want_win || gd.ntiles <= 0) continue;
+          if (on_tc[gi] || gd.taps_smem != want_smem || gd.win != want_win || gd.ntiles <= 0) continue;
           L.fuse_map[nm++] = (int8_t)gi;
           fsmem = std::max(fsmem, (size_t)gd.smem_bytes);
           ftiles = std::max(ftiles, (int)gd.ntiles);
@@ -972,32 +960,18 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
         if (e != cudaSuccess) return cuda_status(e);
         launches_last_++;
       }
-      ng = 0;  // nothing left for the per-group loop
+      for (int gi = 0; gi < ng; ++gi) on_tc[gi] = 1;  // nothing left for the per-group loop
     }
   }
-  // one launch per decimation group, each with its own tile shape and
+  // one launch per remaining FP32 group, each with its own tile shape and
   // shared-memory size (all on `stream`, so they run back to back)
   for (int gi = 0; gi < ng; ++gi) {
     const GroupDesc& gd = L.groups[gi];
-    if (gd.ntiles <= 0) continue;
+    if (gd.ntiles <= 0 || on_tc[gi]) continue;
     const int eg = group_of_d_[gd.D];
     if (!prof_ev_.empty()) {
       cudaEventRecord(prof_ev_[2 * eg], stream);
       prof_hit_[eg] = 1;
-    }
-    if (use_tc_for(eg)) {
-      // groups whose operands do not fit the tensor-core kernel's shared
-      // memory keep the FP32 form (nothing was launched in that case)
-      const int before = tc_groups_last_;
-      const int st = launch_tc_group(eg, d_in, n, out, stream);
-      if (st == FDSP_OK) {
-        if (!prof_ev_.empty()) {
-          cudaEventRecord(prof_ev_[2 * eg + 1], stream);
-          prof_tc_[eg] = tc_groups_last_ > before ? 1 : 0;
-        }
-        continue;
-      }
-      if (st != FDSP_ERR_UNSUPPORTED) return st;
     }
     const size_t smem = (size_t)gd.smem_bytes;
     auto kern = gd.win ? (gd.taps_smem ? poly_fp32_kernel<NB, true, true> : poly_fp32_kernel<NB, false, true>)
@@ -1008,10 +982,7 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
-    if (!prof_ev_.empty()) {
-      cudaEventRecord(prof_ev_[2 * eg + 1], stream);
-      prof_tc_[eg] = 0;
-    }
+    if (!prof_ev_.empty()) cudaEventRecord(prof_ev_[2 * eg + 1], stream);
   }
   if (H_ > 0) {
     hist_update_kernel<<<(H_ + 255) / 256, 256, 0, stream>>>(d_hist_[hist_cur_], in16_ ? nullptr : d_in, in16_,

@@ -2,6 +2,7 @@
 // libfalcon_dsp_gb300.  Nothing here is part of the public C ABI.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -10,6 +11,7 @@
 #include <vector>
 
 #include "fdsp_c.h"
+#include "fdsp_tc_plan.h"
 
 #define FDSP_TRY(expr)              \
   do {                              \
@@ -97,103 +99,34 @@ struct PolyLaunch {
 };
 
 // ---------------------------------------------------------------------------
-// Tensor-core launch: a set of merge sets of one decimation group.
+// Tensor-core launch: every decimation group computed on the tensor cores,
+// planned by tc_plan (fdsp_tc_plan.h).  The whole record travels in the
+// kernel parameter block (no host->device copy per apply).
 // ---------------------------------------------------------------------------
-constexpr int kMaxTcWorkSets = 128;
-constexpr int kMaxTcMsets = 16;
-constexpr int kMaxTcSlots = 256;     // channel slots (Re/Im column pairs) per launch
-
-// One work set (chunk of channels of one (up, down) class x output phase r).
-struct TcWorkSet {
-  const uint8_t* b;      // B records of the work set's tap phase: [ng][T] cores of 128 B (device)
-  const float2* taps32;  // [T][n] FP32 modulated taps (rollover correction)
-  const int16_t* ch;     // channel ids of the chunk (device)
-  int32_t T;             // taps per phase, padded to even
-  int32_t n;             // channels in the chunk
-  int32_t ng;            // 8-column groups of its B (2 columns per channel)
-  int32_t delta;         // window end of row 0 (block relative)
-  int32_t J;             // rows with an output in this launch
-  int32_t U;             // class up rate (output m = r + U j)
-  int32_t r;
-  int32_t o;             // tap offset of its window inside the merge set's window
-  int32_t s0;            // first slot (column pair) inside the merge set's B
-  int32_t pad_;
-};
-
-// Work sets whose windows are merged into one wider matrix product: their
-// taps sit at their own offsets of a common window of Kw taps (zeros
-// elsewhere) and their channels side by side along N.
-struct TcMset {
-  int32_t Kw;            // taps of the merged window (even)
-  int32_t N;             // MMA N: columns, multiple of 16, <= 128
-  int32_t a;             // window start of row 0 inside the staged tile (records)
-  int32_t boff;          // shared-memory byte offset of its B
-  int32_t ws_begin, ws_end;
-  int32_t toff;          // first entry of its A-offset table (multiple of 4)
-  int32_t slot0;         // first entry of its channel slots in TcLaunch::slot
-  int32_t poff;          // shared-memory byte offset of its row-rotation tables, then row-0 counter inputs
-  int32_t pad_[3];
-};
-
-// Per-output constants of one channel slot, read by every output of the
-// slot (kernel parameters: served by the constant cache, so they take no
-// shared-memory bandwidth from the matrix operands).
-struct TcSlotHot {
-  uint32_t om_lo, om_hi;  // NCO turns per sample (2^-64 units; 0: no shift)
-  uint32_t out_lo, out_hi;// output of row 0: channel output + r (row j writes out + U j)
-  uint32_t R;             // counter rollover (0x7fffffff: no shift, or exact path)
-  uint32_t Tm1;           // taps - 1 (0x7fffffff: every output on the exact path)
-  uint32_t U;             // class up rate (output m = r + U j)
-  int32_t J;              // rows with an output (0: padding slot)
-};
-
 struct TcLaunch {
-  const float2* block;
+  CUtensorMap maps[kTcMaxGroups];    // A operand of each group: rows D' samples apart over xhl
+  const float2* block;               // input block (exact rollover path)
   const short2* block16;             // or, when set, the block as complex int16
-  const float2* hist;
-  const uint2* xhl;                  // [history | block] as packed {hi, lo} 16-bit pairs
-  const NcoConst* nco;
-  int* err;                          // set to 1 when a bounded wait gave up
-  int64_t N;
-  int32_t H;
-  int32_t D;
-  int32_t ntiles;                    // 128-row tiles
-  int32_t nmsets;
-  int32_t V;                         // staged phases per tile
-  int32_t Qp;                        // records per staged phase
-  int32_t wrap;                      // 1: a tap's phase is taken mod D (V = D + 1)
-  int32_t B0;                        // block-relative sample of record (0, 0) of tile 0
-  int32_t in_off;                    // shared-memory byte offset of the input buffers
-  int32_t in_bytes;                  // bytes of one input buffer
-  int32_t nbuf;                      // input buffers (1 to 4)
-  int32_t tab_off;                   // shared-memory byte offset of the A-offset tables
-  int32_t raw_off;                   // shared-memory byte offset of the raw span buffer
-  int32_t raw_span;                  // samples of a tile's raw span (0: per-record staging)
-  int32_t nraw;                      // raw span buffers (1 or 2)
-  int32_t epi_groups;                // epilogue warp groups (1 or 4)
-  int32_t raw_stride;                // bytes between raw span buffers
-  int32_t pair;                      // 1: records hold samples 2v, 2v + 1 of a phase pair (even D)
-  int32_t pad_;
-  TcMset ms[kMaxTcMsets];
-  TcSlotHot slot[kMaxTcSlots];
-  TcWorkSet ws[kMaxTcWorkSets];
-  float2* out[kMaxChannels];
-  uint32_t nco_base[kMaxChannels];
+  const float2* hist;                // history (H samples preceding the block)
+  const NcoConst* nco;               // [channels]
+  const float2* const* ctaps;        // per channel: FP32 modulated taps [U][T]
+  uint2* xhl;                        // [history | block | zeros] as {hi, lo} 16-bit parts (prep writes it)
+  uint8_t* bbuf;                     // B images of the merge sets (prep writes them)
+  int* err;                          // bounded-wait failures (mapped host memory)
+  int64_t N;                         // block samples
+  int64_t Lc;                        // samples of the time range each CTA owns
+  int64_t xhl_n;                     // samples of xhl the prep writes
+  int32_t H, G, nmsets, ngroups, stages, stage_bytes;
+  uint32_t poll;                     // polls before a wait gives up (each suspends up to ~2 us)
+  int32_t hold;                      // test hook: the producer issues nothing (every wait runs out)
+  int32_t bprefix[kTcMaxMsets + 1];  // 16-byte pieces of the B images before merge set m
+  TcGroup groups[kTcMaxGroups];
+  TcMset ms[kTcMaxMsets];
+  TcSlot slots[kTcMaxSlots];
+  uint32_t nco_base[kMaxChannels];   // (samples since reset at block[0]) mod R per channel
 };
 
 static_assert(sizeof(TcLaunch) <= 32764, "tensor-core launch must fit the kernel parameter block");
-
-struct TcChunk {
-  int cls;
-  std::vector<int> chans;
-  int T;            // taps per phase, padded to even
-  bool supported;   // T within the tensor-core kernel's limit
-  int ng;           // 8-column groups
-  size_t bbytes;    // bytes of one phase's B: ng * T * 128
-  uint8_t* d_b;     // [U][ng][T] cores of 128 B
-  float2* d_taps32; // [U][T][n]
-  int16_t* d_ch;
-};
 
 // CUDA error -> status, remembering the CUDA code for fdsp_last_cuda_error().
 int cuda_status(cudaError_t e);
@@ -259,7 +192,7 @@ struct EngineGroup {
   int Qt;
   int Qt_default = 0;  // tile rows chosen from the shapes alone
   int use_tc = 1;      // tensor-core form when the precision asks for it (autotuned)
-  int tc_split = 1;    // largest row split of the tensor-core form (autotuned; 1 = none)
+  int tc_split = 32;   // largest row split of the tensor-core form (1 = none)
   int tc_split_used = 1;  // row split of its last tensor-core launch
   int win = 0;         // single-channel long filters: the FP32 kernel's sliding-window form applies
   int Qt_win = 0;      // its tile rows (multiple of 32 x kWinRows)
@@ -304,12 +237,19 @@ class PolyEngine {
   // or one of the split-precision tensor-core forms.
   int set_precision(int mode);
   int precision() const { return precision_; }
-  // 1 when a tensor-core kernel hit its bounded wait since the last reset.
-  int tc_error() const;
-  // Time every decimation group on an n-sample block: the FP32 tile height
-  // among {1/2, 1, 2, 4} x the default, then tensor cores (row split of up
-  // to 1, 2, 4) vs FP32 under a tensor-core precision; keep the fastest per
-  // group.  Resets the stream.
+  // 1 when a tensor-core kernel hit its bounded wait since the last check
+  // (after the caller has synchronised with the apply); clears the flag.
+  int tc_error();
+  // Polls before a tensor-core wait gives up (each suspends up to ~2 us), and
+  // a test hook that makes the next launches' producer issue nothing.
+  void set_tc_wait(uint32_t polls, int hold) {
+    tc_poll_ = polls ? polls : 1u;
+    tc_hold_ = hold;
+  }
+  // Time every decimation group on an n-sample block and keep, per group,
+  // the fastest FP32 tile height among {1/2, 1, 2, 4} x the default (the
+  // tensor-core form runs every group of an apply in one launch and plans its
+  // own tiles).  Resets the stream.
   int autotune(uint64_t n, cudaStream_t stream);
   int num_groups() const { return (int)groups_.size(); }
   // CUDA-graph replay of each apply's launch sequence (captured on the
@@ -324,10 +264,9 @@ class PolyEngine {
     *use_tc = use_tc_for(g) ? 1 : 0;
   }
   int group_tc_split(int g) const { return groups_[g].tc_split_used; }
-  // Largest row split of every group's tensor-core form (1..8); the
-  // autotuner sets it per group.
+  // Largest row split of every group's tensor-core form (1..32).
   int set_tc_split(int s) {
-    if (s < 1 || s > 8) return FDSP_ERR_INVALID_ARG;
+    if (s < 1 || s > 32) return FDSP_ERR_INVALID_ARG;
     for (auto& g : groups_) g.tc_split = s;
     return FDSP_OK;
   }
@@ -337,16 +276,20 @@ class PolyEngine {
   int launch(const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream);
   int build_tc(int fmt);
   void free_tc();
-  bool group_tc_ok(int gi) const;
-  int groups_idx_of_class(int cls) const;
-  int launch_tc_group(int gi, const float2* d_in, uint64_t n, float2* const* out, cudaStream_t stream);
-  int prepare_tc_input(const float2* d_in, uint64_t n, cudaStream_t stream);
-  uint2* d_xhl_ = nullptr;          // scratch: pre-split input of the current apply
-  size_t xhl_cap_ = 0;
+  int launch_tc(const float2* d_in, uint64_t n, float2* const* out, const std::vector<int>& tc_groups,
+                std::vector<int>& fallback, cudaStream_t stream);
   int precision_ = FDSP_PRECISION_FP32;
   int tc_fmt_ = 0;
-  std::vector<TcChunk> tc_chunks_;
-  int* d_err_ = nullptr;
+  float2* d_ctaps_ = nullptr;          // FP32 modulated taps of every channel, [U][T] each
+  const float2** d_ctab_ = nullptr;    // per channel: its taps in d_ctaps_
+  uint2* d_xhl_ = nullptr;             // scratch: split input of the current apply
+  size_t xhl_cap_ = 0;                 // samples
+  uint8_t* d_bbuf_ = nullptr;          // scratch: B images of the current apply
+  size_t bbuf_cap_ = 0;
+  int* h_err_ = nullptr;               // bounded-wait failures, mapped host memory
+  int* d_err_ = nullptr;               // its device address
+  uint32_t tc_poll_ = 1u << 20;
+  int tc_hold_ = 0;
   int num_sms_ = 0;
 
   uint32_t fs_ = 0;
@@ -373,7 +316,6 @@ class PolyEngine {
   bool use_tc_for(int eg) const;
   std::vector<cudaEvent_t> prof_ev_;   // autotuning: [2 g] / [2 g + 1] around group g
   std::vector<int> prof_hit_;          // group g launched in the timed apply
-  std::vector<int> prof_tc_;           // group g ran on the tensor-core kernel
 };
 
 // NCO constants of a (fs, f) pair, following falcon_dsp_freq_shift.cc:194-235.

@@ -1,201 +1,269 @@
-// Launch planning of the tensor-core polyphase kernel (host only): merge
-// sets, staging geometry, shared-memory budget and the row split.  Kept
-// apart from the kernel so that its bounds can be checked on the CPU
-// (tests/cpp/tc_plan_check.cc restates the kernel's shared-memory indexing
-// over these plans).
+// Launch planning of the tensor-core filter-bank kernel (host only).
+//
+// One launch covers every decimation group computed on the tensor cores.
+// Per group the output rows (windows ending D apart) become 128-row tiles of
+// a matrix product Y = A B:
+//
+//   A[j][k]  input sample  j D' + a + k  of [history | block], split into
+//            16-bit {hi, lo} parts: 4 K elements per sample
+//            (re_hi, im_hi, re_lo, im_lo), a Hankel matrix that TMA loads
+//            16 samples (128 bytes) at a time through a tensor map whose
+//            row stride is D' samples;
+//   B[k][n]  the NCO-modulated taps of each output stream ("slot") at its
+//            offset inside the merged window, hi taps in columns [0, 2 NS),
+//            lo taps in [2 NS, 4 NS) (Re, Im per slot): the epilogue adds
+//            the two halves, so each output is (x_hi + x_lo)(g_hi + g_lo)
+//            with FP32 accumulation.
+//
+// A slot is one output class of one channel: output m = r + U j of channel
+// c uses tap phase phi and the window ending at delta + j D (block relative).
+// A row split S (rows j = S i + b become S slots whose rows are S D apart)
+// widens groups with few slots, and makes an odd D even (TMA strides are
+// multiples of 16 bytes = 2 samples).  Slots sorted by window start are
+// merged greedily into merge sets ("msets") of <= 32 slots whose windows
+// span at most cap(T) taps; an mset's window starts on an even sample (TMA
+// x coordinates are multiples of 16 bytes) and is chunked in 16 taps.
+//
+// Kept apart from the kernel so that its bounds can be checked on the CPU
+// (tests/cpp/tc_plan_check.cc).
 #pragma once
 
 #include <stdint.h>
 
 #include <algorithm>
+#include <climits>
 #include <vector>
 
-#include "fdsp_internal.h"
+#if defined(__CUDACC__)
+#define FDSP_HD __host__ __device__
+#else
+#define FDSP_HD
+#endif
 
 namespace fdsp {
 
-constexpr uint32_t kTcDCols = 128;    // accumulator columns per slot (N <= 128)
-constexpr int kTcMaxKw = 128;         // taps of a merged window (before pair rounding)
-constexpr size_t kTcSmemMax = 222 * 1024;  // + ~4.3 KB static (barriers, epilogue phasors) <= 227 KB
-constexpr int kTcMaxBuf = 4;          // input buffers
-constexpr size_t kTcRawMax = 48 * 1024; // raw span buffer (bulk-copy staging) at most
+constexpr int kTcMaxGroups = 16;
+constexpr int kTcMaxMsets = 64;
+constexpr int kTcMaxSlots = 512;
+constexpr int kTcRows = 128;           // rows per tile (MMA M)
+constexpr int kTcChunkTaps = 16;       // taps per K chunk: 128 bytes of A per row
+constexpr int kTcTileBytes = kTcRows * 128;
+constexpr int kTcMsetSlots = 32;       // slots per merge set (N = 4 NS <= 128)
+constexpr int kTcStageMaxBytes = 49152;
+constexpr int kTcSmemDyn = 225 * 1024; // dynamic shared memory ceiling (227 KB minus static and alignment)
+constexpr int kTcMaxStages = 6;
 
-struct TcChunk;
-
-// One work set of the group for this apply, before merging.
-struct TcWsPlan {
-  const TcChunk* ch;
-  int T = 0;      // taps per phase of its chunk (even)
-  int n = 0;      // channels of its chunk
-  uint32_t phi;   // tap phase
-  int64_t delta;  // window end of row 0
-  int64_t J;
-  uint32_t U, r;
+// ---- launch records (kernel parameters; shared with the device code) -----
+struct TcGroup {
+  int32_t D;        // row stride D' = S D (samples, even)
+  int32_t S;        // row split
+  int32_t pad_[2];
 };
 
-struct TcMsetPlan {
-  std::vector<int> ws;   // indices into the work-set list
-  int64_t E = 0;         // latest window end
-  int64_t S0 = 0;        // earliest window start of its work sets
-  int64_t S = 0;         // merged window start (row 0): E - Kw + 1, Kw rounded up to even
-  int Kw = 0;
-  int cols = 0;          // 8-column groups x 8
+struct TcMset {
+  uint64_t b;       // device address of its B image: [nchunks][N][128 B]
+  int32_t a;        // window start of row 0 in [history | block] samples (even)
+  int32_t items;    // work items (R tiles each)
+  int16_t group, slot0, NS, nchunks, R, pad_;
+  int32_t ntiles;   // 128-row tiles with an output
 };
 
-struct TcLaunchPlan {
-  std::vector<int> ms;   // merge-set indices
-  int nws = 0, nslots = 0;
-  int64_t B0 = 0;
-  int V = 0, Qp = 0, wrap = 0, nbuf = 1;
-  int pair = 0;          // 1: pair records (even D: 16-byte records of two samples)
-  int raw_span = 0;      // > 0: tiles staged through one bulk copy of their input span
-  int nraw = 0;          // raw span buffers (1 or 2)
-  size_t b_bytes = 0, meta_bytes = 0, tab_bytes = 0, in_bytes = 0, raw_bytes = 0, raw_stride = 0;
+struct TcSlot {
+  uint64_t out;     // float2*: output of row 0 (channel output + r)
+  int32_t w0;       // window start of row 0, block relative (delta - T + 1)
+  int32_t J;        // rows with an output (0: padding slot)
+  uint16_t ch;      // channel
+  uint16_t T;       // taps per phase
+  uint16_t U;       // output stride (up rate x row split)
+  uint16_t o;       // window start inside the merge set's window (taps)
+  uint16_t phi;     // tap phase
+  uint16_t pad_[3];
+};
+static_assert(sizeof(TcSlot) == 32, "slot record");
+static_assert(sizeof(TcMset) == 32, "merge-set record");
+
+// ---- planner input ----------------------------------------------------------
+struct TcSlotIn {
+  int ch, T, U, r, phi;
+  int64_t delta;    // window end of row 0 (block relative)
+  int64_t J;        // rows with an output this apply
+};
+struct TcGroupIn {
+  int D;
+  int max_split;    // largest row split allowed (power of two, 1..32)
+  std::vector<TcSlotIn> slots;
 };
 
-// [B of each merge set | slot constants | A-offset tables | raw span | input buffers]
-inline size_t tc_smem_need(const TcLaunchPlan& p, int nbuf) {
-  return ((p.b_bytes + p.meta_bytes + p.tab_bytes + 127) & ~(size_t)127) + p.raw_bytes + (size_t)nbuf * p.in_bytes;
+struct TcPlanGroup {
+  int D, S;
+  int64_t Wx;       // samples a row of its tensor map spans (max over its msets of (a mod D') + Kw)
+};
+
+struct TcPlan {
+  std::vector<TcPlanGroup> groups;
+  std::vector<TcMset> ms;         // b = byte offset into the B buffer (the engine adds the base)
+  std::vector<TcSlot> slots;      // out = 0 (the engine fills it)
+  std::vector<int> slot_r;        // output offset r of each slot (for the out pointer)
+  size_t b_bytes = 0;
+  int64_t xhl_samples = 0;        // [history | block | zero pad] samples the split writes
+  int stages = 0, stage_bytes = 0, smem = 0;
+  int G = 0;                      // grid (CTAs)
+  int64_t Lc = 0;                 // samples of the time range each CTA owns
+  int64_t items = 0;
+};
+
+inline int64_t tc_round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+// Window span a merge set may reach for its longest filter T: a quarter more
+// than T, at least T + 17 (padding slots' windows to one chunk costs less
+// than one more merge set).
+inline int64_t tc_window_cap(int64_t T) { return T + std::max<int64_t>(17, T / 4); }
+
+// Row split of a group: odd D needs S even; beyond that the split doubles
+// while the slots still fill at most one merge set and the windows of the
+// split rows stay within the cap of the longest filter.
+inline int tc_choose_split(int D, int nslots, int Tmax, int max_split) {
+  int S = (D & 1) ? 2 : 1;
+  while (S * 2 <= max_split && (int64_t)nslots * S * 2 <= kTcMsetSlots &&
+         (int64_t)(2 * S - 1) * D <= tc_window_cap(Tmax) - Tmax)
+    S *= 2;
+  return S;
 }
 
-// Staging geometry of a launch covering merge sets p.ms.
-inline void tc_geometry(const std::vector<TcMsetPlan>& msets, TcLaunchPlan& p, uint32_t D, int raw_bufs = 2) {
-  const int tpm = p.pair ? 4 : 2;  // taps per MMA
-  p.B0 = INT64_MAX;
-  p.b_bytes = p.meta_bytes = p.tab_bytes = 0;
-  p.nws = p.nslots = 0;
-  for (int m : p.ms) {
-    p.B0 = std::min(p.B0, msets[m].S);
-    const int N = ((msets[m].cols + 15) / 16) * 16;
-    p.nws += (int)msets[m].ws.size();
-    p.nslots += N / 2;
-    p.b_bytes += (size_t)N * msets[m].Kw * 16;
-    p.meta_bytes += (size_t)(N / 2) * (8 * sizeof(float2) + 9 * sizeof(uint32_t));
-    p.tab_bytes += (size_t)((msets[m].Kw / tpm + 3) & ~3) * 4;
-  }
-  int64_t W = 0;
-  for (int m : p.ms) W = std::max<int64_t>(W, msets[m].S - p.B0 + msets[m].Kw);
-  p.wrap = W > (int64_t)D ? 1 : 0;
-  if (p.pair)
-    p.V = p.wrap ? (int)D / 2 + 1 : (int)W / 2;
-  else
-    p.V = p.wrap ? (int)D + 1 : (int)W;
-  p.Qp = p.wrap ? 128 + (int)((W - 1) / D) : 128;
-  // wrapped windows read (nearly) every sample of the tile's span: stage
-  // them with one bulk copy when the span is small enough (Qp odd keeps the
-  // record writes free of bank conflicts)
-  p.raw_span = 0;
-  p.nraw = 0;
-  p.raw_bytes = p.raw_stride = 0;
-  if (p.wrap && raw_bufs > 0) {
-    const int qp = p.Qp | 1;
-    const size_t span = (size_t)qp * D + (p.pair ? 2 : 1);
-    const size_t bytes = (((span + 2) * 8) + 127) & ~(size_t)127;
-    if (bytes <= kTcRawMax) {
-      p.Qp = qp;
-      p.raw_span = (int)span;
-      p.nraw = raw_bufs;
-      p.raw_stride = bytes;
-      p.raw_bytes = bytes * (size_t)raw_bufs;
-    }
-  }
-  p.in_bytes = (((size_t)p.V * p.Qp * 16) + 127) & ~(size_t)127;
-}
-
-// Merge sets: consecutive (by window end) work sets while N <= cap columns
-// and the merged window stays within kTcMaxKw taps.
-inline std::vector<TcMsetPlan> tc_merge(const std::vector<TcWsPlan>& wl, const std::vector<int>& order, int cap) {
-  std::vector<TcMsetPlan> msets;
-  for (int wi : order) {
-    const TcWsPlan& w = wl[wi];
-    const int64_t s = w.delta - w.T + 1;
-    const int cols = 2 * w.n;
-    bool joined = false;
-    if (!msets.empty()) {
-      TcMsetPlan& m = msets.back();
-      const int64_t E = std::max(m.E, w.delta);
-      const int64_t S0 = std::min(m.S0, s);
-      const int Kw = (int)(((E - S0 + 1) + 1) & ~1LL);
-      if (m.cols + cols <= cap && Kw <= kTcMaxKw) {
-        m.ws.push_back(wi);
-        m.E = E;
-        m.S0 = S0;
-        m.S = E - Kw + 1;
-        m.Kw = Kw;
-        m.cols += cols;
-        joined = true;
+// Returns 0 on success, -1 when the apply exceeds a launch's record limits
+// (the caller keeps those groups on the FP32 kernel).
+inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_sms, TcPlan& p) {
+  p = TcPlan();
+  int64_t wx_max = 0;
+  for (const TcGroupIn& g : gin) {
+    if (g.slots.empty()) continue;
+    int Tmax = 1;
+    for (const TcSlotIn& s : g.slots) Tmax = std::max(Tmax, s.T);
+    const int S = tc_choose_split(g.D, (int)g.slots.size(), Tmax, std::max(1, g.max_split));
+    const int64_t Dp = (int64_t)S * g.D;
+    // slots of the split rows
+    struct X {
+      TcSlotIn s;
+      int64_t start;  // window start of row 0 (block relative)
+    };
+    std::vector<X> xs;
+    for (const TcSlotIn& s : g.slots) {
+      for (int b = 0; b < S; ++b) {
+        if (s.J <= b) continue;
+        X x;
+        x.s = s;
+        x.s.delta = s.delta + (int64_t)b * g.D;
+        x.s.J = (s.J - b + S - 1) / S;
+        x.s.U = s.U * S;
+        x.s.r = s.r + b * s.U;
+        x.start = x.s.delta - s.T + 1;
+        xs.push_back(x);
       }
     }
-    if (!joined) {
-      TcMsetPlan m;
-      m.ws.push_back(wi);
-      m.E = w.delta;
-      m.Kw = w.T;
-      m.S0 = s;
-      m.S = m.E - m.Kw + 1;
-      m.cols = cols;
-      msets.push_back(m);
-    }
-  }
-  return msets;
-}
-
-// Pair records (even D) read taps four at a time from records of two
-// samples: every merged window starts on an even sample and spans a multiple
-// of four taps (the extra taps are zero).
-inline void tc_pair_windows(std::vector<TcMsetPlan>& msets) {
-  for (auto& m : msets) {
-    const int64_t S = m.S0 & ~1LL;  // even, at or before every work set's window start
-    m.Kw = (int)(((m.E - S + 1) + 3) & ~3LL);
-    m.S = S;
-  }
-}
-
-// Launches: consecutive merge sets while shared memory allows; false when a
-// single merge set does not fit.
-inline bool tc_pack(const std::vector<TcMsetPlan>& msets, uint32_t D, int pair, std::vector<TcLaunchPlan>& plans) {
-  plans.clear();
-  for (int mi = 0; mi < (int)msets.size(); ++mi) {
-    bool joined = false;
-    if (!plans.empty() && (int)plans.back().ms.size() < kMaxTcMsets) {
-      TcLaunchPlan p = plans.back();
-      p.ms.push_back(mi);
-      tc_geometry(msets, p, D);
-      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, 1);
-      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, 0);
-      if (tc_smem_need(p, 1) <= kTcSmemMax && p.nws <= kMaxTcWorkSets && p.nslots <= kMaxTcSlots) {
-        plans.back() = p;
-        joined = true;
+    if (xs.empty()) continue;
+    std::stable_sort(xs.begin(), xs.end(), [](const X& a, const X& b) {
+      return a.start != b.start ? a.start < b.start : a.s.delta < b.s.delta;
+    });
+    if ((int)p.groups.size() >= kTcMaxGroups) return -1;
+    const int gi = (int)p.groups.size();
+    TcPlanGroup pg;
+    pg.D = (int)Dp;
+    pg.S = S;
+    pg.Wx = 0;
+    size_t i = 0;
+    while (i < xs.size()) {
+      // window start of the merge set in [history | block] samples, even
+      int64_t a = xs[i].start + H;
+      if (a & 1) a -= 1;
+      int64_t end = xs[i].s.delta, tm = xs[i].s.T;
+      size_t j = i + 1;
+      while (j < xs.size() && (int)(j - i) < kTcMsetSlots) {
+        const int64_t e2 = std::max(end, xs[j].s.delta), t2 = std::max<int64_t>(tm, xs[j].s.T);
+        if (e2 + H - a + 1 > tc_window_cap(t2)) break;
+        end = e2;
+        tm = t2;
+        ++j;
       }
+      const int64_t Kw = end + H - a + 1;
+      const int nreal = (int)(j - i);
+      // record field ranges (16-bit taps, strides and offsets)
+      if (Kw > 65535 || tm > 65535) return -1;
+      for (size_t q = i; q < j; ++q)
+        if (xs[q].s.U > 65535 || xs[q].s.phi > 65535 || xs[q].s.J > INT32_MAX) return -1;
+      const int NS = (int)tc_round_up(nreal, 8);
+      if ((int)p.ms.size() >= kTcMaxMsets || (int)p.slots.size() + NS > kTcMaxSlots) return -1;
+      TcMset m{};
+      m.a = (int32_t)a;
+      m.group = (int16_t)gi;
+      m.slot0 = (int16_t)p.slots.size();
+      m.NS = (int16_t)NS;
+      m.nchunks = (int16_t)((Kw + kTcChunkTaps - 1) / kTcChunkTaps);
+      m.R = (int16_t)(4 * NS <= 128 ? 2 : 1);
+      int64_t Jmax = 0;
+      for (size_t q = i; q < j; ++q) {
+        const X& x = xs[q];
+        TcSlot s{};
+        s.w0 = (int32_t)x.start;
+        s.J = (int32_t)x.s.J;
+        s.ch = (uint16_t)x.s.ch;
+        s.T = (uint16_t)x.s.T;
+        s.U = (uint16_t)x.s.U;
+        s.o = (uint16_t)(x.start + H - a);
+        s.phi = (uint16_t)x.s.phi;
+        p.slots.push_back(s);
+        p.slot_r.push_back(x.s.r);
+        Jmax = std::max(Jmax, x.s.J);
+      }
+      for (int q = nreal; q < NS; ++q) {
+        p.slots.push_back(TcSlot{});
+        p.slot_r.push_back(0);
+      }
+      m.ntiles = (int32_t)((Jmax + kTcRows - 1) / kTcRows);
+      m.items = (m.ntiles + m.R - 1) / m.R;
+      m.b = p.b_bytes;
+      p.b_bytes += (size_t)tc_round_up((int64_t)m.nchunks * 4 * NS * 128, 1024);
+      pg.Wx = std::max<int64_t>(pg.Wx, a % Dp + (int64_t)m.nchunks * kTcChunkTaps);
+      p.ms.push_back(m);
+      i = j;
     }
-    if (!joined) {
-      TcLaunchPlan p;
-      p.pair = pair;
-      p.ms.push_back(mi);
-      tc_geometry(msets, p, D);
-      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, 1);
-      if (tc_smem_need(p, 1) > kTcSmemMax) tc_geometry(msets, p, D, 0);
-      if (tc_smem_need(p, 1) > kTcSmemMax || p.nws > kMaxTcWorkSets || p.nslots > kMaxTcSlots) return false;
-      plans.push_back(p);
-    }
+    wx_max = std::max(wx_max, pg.Wx);
+    p.groups.push_back(pg);
   }
-  for (auto& p : plans) {
-    p.nbuf = 1;
-    while (p.nbuf < kTcMaxBuf && tc_smem_need(p, p.nbuf + 1) <= kTcSmemMax) p.nbuf++;
+  if (p.ms.empty()) return 0;
+  // the split writes [history | block] and a zero tail: every row a tensor
+  // map can address ((rows - 1) D' + Wx samples) stays inside it
+  p.xhl_samples = tc_round_up(N + H + wx_max + 16, 16);
+  // pipeline stages: R A tiles + one B chunk each
+  int sb = 0;
+  for (const TcMset& m : p.ms)
+    sb = std::max<int>(sb, m.R * kTcTileBytes + (int)tc_round_up((int64_t)4 * m.NS * 128, 1024));
+  if (sb > kTcStageMaxBytes) return -1;
+  p.stage_bytes = sb;
+  p.stages = std::min(kTcMaxStages, (kTcSmemDyn - 1024) / sb);
+  if (p.stages < 2) return -1;
+  p.smem = p.stages * sb + 1024;
+  // schedule: each CTA owns a contiguous range of input samples and runs the
+  // items of every merge set that start in it, in input order
+  int64_t umax = 0;
+  for (const TcMset& m : p.ms) {
+    const int64_t P = (int64_t)m.R * kTcRows * p.groups[m.group].D;
+    umax = std::max<int64_t>(umax, m.a + (int64_t)m.items * P);
+    p.items += m.items;
   }
-  return true;
+  p.G = (int)std::max<int64_t>(1, std::min<int64_t>(num_sms, p.items));
+  p.Lc = (umax + p.G - 1) / p.G;
+  return 0;
 }
 
-// Row split of a group whose channel columns (2 x channels x up rate, over
-// its chunks) are few: the largest S <= limit (at most 8) with S x cols
-// columns in one product and a merged window of T + (S - 1) D taps (plus
-// pair rounding) within kTcMaxKw.
-inline uint32_t tc_row_split(int cols, int tmax, uint32_t D, int limit) {
-  uint32_t split = 1;
-  while ((int)split < std::min(limit, 8) && cols > 0 && cols * (int)(split + 1) <= (int)kTcDCols &&
-         (int64_t)tmax + (int64_t)split * D + 4 <= kTcMaxKw)
-    ++split;
-  return split;
+// Item range [first, last) of merge set m owned by CTA b (shared with the
+// device code: every role walks the same sequence).
+FDSP_HD inline void tc_item_range(int64_t a, int64_t P, int64_t items, int64_t Lc, int b, int G, int64_t* first,
+                          int64_t* last) {
+  const int64_t v0 = (int64_t)b * Lc - a, v1 = (int64_t)(b + 1) * Lc - a;
+  int64_t f = v0 <= 0 ? 0 : (v0 + P - 1) / P;
+  int64_t l = v1 <= 0 ? 0 : (v1 + P - 1) / P;
+  *first = f < items ? f : items;
+  *last = (b == G - 1) ? items : (l < items ? l : items);
 }
 
 }  // namespace fdsp

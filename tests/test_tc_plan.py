@@ -1,13 +1,14 @@
-"""Bounds of the tensor-core kernel's launch plans, checked on the CPU.
+"""Bounds and coverage of the tensor-core planner, checked on the CPU.
 
-tests/cpp/tc_plan_check.cc plans random decimation groups (1-4 classes of up
-rates 1-4, 2-64 taps, 1-32 channels, D 2-400, row-split limits 1-8) with the
-library's own planner (libfalcon_dsp_gb300/csrc/fdsp_tc_plan.h: row split,
-merge sets, pair windows, launches) and checks every shared-memory read the
-kernel derives from a plan against the plan's sizes: the A operand's records
-of each MMA, the taps of each work set inside its merged window, the staged
-span of the bulk copy, and the shared-memory budget of the chosen buffer
-count.  No GPU is involved.
+tests/cpp/tc_plan_check.cc plans random channel sets (1-6 decimation groups
+of 1-3 classes, up rates 1-4, 1-70 taps per phase, D 1-400, and every 17th
+case a long single-channel FIR of 200-5000 taps) with the library's own
+planner (libfalcon_dsp_gb300/csrc/fdsp_tc_plan.h) and checks what the
+kernels derive from each plan: TMA coordinates and tensor-map rows inside the
+split buffer, each output's window inside [history | block] and inside its
+merge set's chunked window, B images, stages and tensor-memory columns inside
+their budgets, per-CTA item ranges partitioning every merge set, and every
+output of every channel written exactly once.  No GPU is involved.
 """
 import os
 import shutil
@@ -17,21 +18,18 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "tc_plan_check.cc")
-CUDA_INC = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
 
 
-def test_tc_launch_plans_stay_in_bounds(tmp_path):
+def test_tc_plans_stay_in_bounds_and_cover_every_output(tmp_path):
     cxx = shutil.which("g++")
     if cxx is None:
         pytest.skip("g++ not available")
-    if not os.path.exists(os.path.join(CUDA_INC, "cuda_runtime.h")):
-        pytest.skip("CUDA headers not available")
     exe = str(tmp_path / "tc_plan_check")
     cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "libfalcon_dsp_gb300", "csrc"),
-           "-I", os.path.join(ROOT, "include"), "-I", CUDA_INC, SRC, "-o", exe]
+           SRC, "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    r = subprocess.run([exe, "20000"], capture_output=True, text=True, timeout=120)
+    r = subprocess.run([exe, "2000"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
-    ok, cases, launches, mmas = r.stdout.split()
-    assert ok == "ok" and int(cases) == 20000 and int(launches) > 20000 and int(mmas) > 100000
+    ok, cases, msets, items = r.stdout.split()
+    assert ok == "ok" and int(cases) == 2000 and int(msets) > 5000 and int(items) > 100000
