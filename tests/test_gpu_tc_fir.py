@@ -6,7 +6,8 @@ with FP32 accumulation.
 Bounds: >= 60 dB SNR against an FP64 evaluation of the same filter on every
 block of a streaming run (ragged block sizes, state carried); output counts
 equal the input counts; the tensor-core kernel really ran; the FP32 form
-still meets 1e-5 relative RMS against the oracle after switching back.
+still meets 1e-5 relative RMS against the oracle after switching back and a
+reset.
 """
 import numpy as np
 import pytest
@@ -43,8 +44,10 @@ def test_tc_fir_streaming_snr(mode, ntaps):
         assert _snr_db(y, r) >= 60.0, (i, _snr_db(y, r))
         if blk.size > 100000:
             assert f.tc_groups() == 1
-    # back to FP32: a fresh stream within the FIR bound
+    # back to FP32 (the streaming state carries over): a fresh stream after a
+    # reset within the FIR bound
     f.set_precision("fp32")
+    f.reset_state()
     y = f.apply(x[:50000])
     assert rel_rms(y, O.FIR(h).apply(x[:50000])) <= 1e-5
 
