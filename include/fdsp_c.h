@@ -198,6 +198,13 @@ int fdsp_channelizer_status(fdsp_channelizer *h, fdsp_stream_t stream);
  * withhold_copies != 0 makes later launches issue no operand copies, so every
  * wait runs out: a test hook for the timeout path, never for production. */
 int fdsp_channelizer_set_tc_wait(fdsp_channelizer *h, uint32_t max_polls, int withhold_copies);
+/* Kernel timing (diagnostics, no counterpart in the reference): while
+ * enabled, applies launch directly (no graph) and each filter-bank launch
+ * (tensor-core or FP32 kernel) is bracketed by CUDA events on the apply's
+ * stream; enabling restarts the record.  read: synchronises and returns the
+ * summed milliseconds and the number of timed launches. */
+int fdsp_channelizer_profile(fdsp_channelizer *h, int enable);
+int fdsp_channelizer_profile_read(fdsp_channelizer *h, double *ms, uint32_t *launches);
 /* Kernel launches the most recent apply enqueued (diagnostics, profiling). */
 int fdsp_channelizer_kernel_launches(const fdsp_channelizer *h, uint32_t *n);
 /* Decimation groups that the most recent apply computed on the tensor-core

@@ -227,6 +227,17 @@ int fdsp_channelizer_set_tc_wait(fdsp_channelizer* h, uint32_t max_polls, int wi
   return FDSP_OK;
 }
 
+int fdsp_channelizer_profile(fdsp_channelizer* h, int enable) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  h->eng.set_profile(enable != 0);
+  return FDSP_OK;
+}
+
+int fdsp_channelizer_profile_read(fdsp_channelizer* h, double* ms, uint32_t* launches) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  return h->eng.read_profile(ms, launches);
+}
+
 int fdsp_channelizer_apply_ci16(fdsp_channelizer* h, const int16_t* d_in, uint64_t n_in, fdsp_cf32* const* d_out,
                                 const uint64_t* out_cap, uint64_t* n_out, fdsp_stream_t stream) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;

@@ -457,6 +457,8 @@ NcoConst make_nco(uint32_t fs, int32_t f) {
 
 PolyEngine::~PolyEngine() {
   if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  for (auto e : kprof_ev_)
+    if (e) cudaEventDestroy(e);
   free_tc();
   for (auto& b : batches_) {
     if (b.d_taps) cudaFree(b.d_taps);
@@ -714,6 +716,35 @@ void PolyEngine::set_graph(bool on) {
   }
 }
 
+void PolyEngine::set_profile(bool on) {
+  kprof_ = on;
+  kprof_used_ = 0;
+}
+
+cudaEvent_t PolyEngine::kprof_event() {
+  if (kprof_used_ == kprof_ev_.size()) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    kprof_ev_.push_back(e);
+  }
+  return kprof_ev_[kprof_used_++];
+}
+
+int PolyEngine::read_profile(double* ms, uint32_t* launches) {
+  if (!ms || !launches) return FDSP_ERR_INVALID_ARG;
+  *ms = 0.0;
+  *launches = 0;
+  for (size_t i = 0; i + 1 < kprof_used_; i += 2) {
+    if (!kprof_ev_[i] || !kprof_ev_[i + 1]) continue;
+    FDSP_TRY(cuda_status(cudaEventSynchronize(kprof_ev_[i + 1])));
+    float t = 0.f;
+    FDSP_TRY(cuda_status(cudaEventElapsedTime(&t, kprof_ev_[i], kprof_ev_[i + 1])));
+    *ms += t;
+    ++*launches;
+  }
+  return FDSP_OK;
+}
+
 bool PolyEngine::use_tc_for(int eg) const {
   if (precision_ == FDSP_PRECISION_FP32 || force_ == 0) return false;
   return force_ == 1 || groups_[eg].use_tc != 0;
@@ -955,7 +986,9 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
                              : (want_smem ? poly_fp32_kernel<NB, true, false> : poly_fp32_kernel<NB, false, false>);
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
         if (e != cudaSuccess) return cuda_status(e);
+        if (kprof_) cudaEventRecord(kprof_event(), stream);
         kern<<<dim3((unsigned)ftiles, (unsigned)(nm - first)), kThreads, fsmem, stream>>>(L, -1 - first);
+        if (kprof_) cudaEventRecord(kprof_event(), stream);
         e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_status(e);
         launches_last_++;
@@ -978,7 +1011,9 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
                        : (gd.taps_smem ? poly_fp32_kernel<NB, true, false> : poly_fp32_kernel<NB, false, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e);
+    if (kprof_) cudaEventRecord(kprof_event(), stream);
     kern<<<(unsigned)gd.ntiles, kThreads, smem, stream>>>(L, gi);
+    if (kprof_) cudaEventRecord(kprof_event(), stream);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
@@ -1019,7 +1054,8 @@ int PolyEngine::apply(const float2* d_in, uint64_t n, float2* const* out, const 
   }
   if (n == 0) return FDSP_OK;
   cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
-  const bool graph = use_graph_ && stream != nullptr && cudaStreamIsCapturing(stream, &capturing) == cudaSuccess &&
+  const bool graph = use_graph_ && !kprof_ && stream != nullptr &&
+                     cudaStreamIsCapturing(stream, &capturing) == cudaSuccess &&
                      capturing == cudaStreamCaptureStatusNone;
   if (graph) {
     const cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed);

@@ -582,9 +582,11 @@ int PolyEngine::tc_error() {
 }
 
 // Plans and enqueues the tensor-core form of the groups in `tc_groups`
-// (engine group indices): one prep launch (input split + B images) and one
-// filter-bank launch.  Groups the plan cannot hold are returned in
-// `fallback` for the FP32 kernel.
+// (engine group indices).  Groups are packed greedily into launches whose
+// records fit the kernel parameter block; per launch one prep (the first
+// also splits the input, which every launch then reads) and one
+// filter-bank launch.  Groups no launch can hold are returned in `fallback`
+// for the FP32 kernel.
 int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, const std::vector<int>& tc_groups,
                           std::vector<int>& fallback, cudaStream_t stream) {
   fallback.clear();
@@ -627,99 +629,141 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev);
     if (num_sms_ <= 0) num_sms_ = 1;
   }
-  TcPlan plan;
-  if (tc_plan(gin, (int64_t)n, H_, num_sms_, plan) != 0) {
-    fallback = tc_groups;
-    return FDSP_OK;
+  // pack groups into launches
+  std::vector<std::vector<int>> packs;  // indices into gin
+  std::vector<TcPlan> plans;
+  {
+    std::vector<int> cur;
+    TcPlan cur_plan;
+    auto plan_of = [&](const std::vector<int>& idx, TcPlan& p) {
+      std::vector<TcGroupIn> sub;
+      for (int i : idx) sub.push_back(gin[i]);
+      return tc_plan(sub, (int64_t)n, H_, num_sms_, p) == 0;
+    };
+    for (int i = 0; i < (int)gin.size(); ++i) {
+      std::vector<int> trial = cur;
+      trial.push_back(i);
+      TcPlan p;
+      if (plan_of(trial, p)) {
+        cur = trial;
+        cur_plan = std::move(p);
+        continue;
+      }
+      if (!cur.empty()) {
+        packs.push_back(cur);
+        plans.push_back(std::move(cur_plan));
+      }
+      cur.assign(1, i);
+      if (!plan_of(cur, cur_plan)) {
+        fallback.push_back(gmap[i]);
+        cur.clear();
+      }
+    }
+    if (!cur.empty()) {
+      packs.push_back(cur);
+      plans.push_back(std::move(cur_plan));
+    }
   }
-  if (plan.ms.empty()) return FDSP_OK;
-  // scratch: split input and B images (grow only)
-  if ((size_t)plan.xhl_samples > xhl_cap_) {
+  if (plans.empty()) return FDSP_OK;
+  // scratch: split input and B images (grow only; launches run in stream
+  // order, so they share one B buffer)
+  int64_t xhl_need = 0;
+  size_t b_need = 0;
+  for (const TcPlan& p : plans) {
+    xhl_need = std::max(xhl_need, p.xhl_samples);
+    b_need = std::max(b_need, p.b_bytes);
+  }
+  if ((size_t)xhl_need > xhl_cap_) {
     if (d_xhl_) cudaFree(d_xhl_);
     d_xhl_ = nullptr;
     xhl_cap_ = 0;
-    FDSP_TRY(cuda_status(cudaMalloc(&d_xhl_, (size_t)plan.xhl_samples * sizeof(uint2))));
-    xhl_cap_ = (size_t)plan.xhl_samples;
+    FDSP_TRY(cuda_status(cudaMalloc(&d_xhl_, (size_t)xhl_need * sizeof(uint2))));
+    xhl_cap_ = (size_t)xhl_need;
   }
-  if (plan.b_bytes > bbuf_cap_) {
+  if (b_need > bbuf_cap_) {
     if (d_bbuf_) cudaFree(d_bbuf_);
     d_bbuf_ = nullptr;
     bbuf_cap_ = 0;
-    FDSP_TRY(cuda_status(cudaMalloc(&d_bbuf_, plan.b_bytes)));
-    bbuf_cap_ = plan.b_bytes;
-  }
-  static thread_local TcLaunch L;
-  std::memset(&L, 0, sizeof(L));
-  L.block = in16_ ? nullptr : d_in;
-  L.block16 = in16_;
-  L.hist = d_hist_[hist_cur_];
-  L.nco = d_nco_;
-  L.ctaps = d_ctab_;
-  L.xhl = d_xhl_;
-  L.bbuf = d_bbuf_;
-  L.err = d_err_;
-  L.N = (int64_t)n;
-  L.Lc = plan.Lc;
-  L.xhl_n = plan.xhl_samples;
-  L.H = H_;
-  L.G = plan.G;
-  L.nmsets = (int32_t)plan.ms.size();
-  L.ngroups = (int32_t)plan.groups.size();
-  L.stages = plan.stages;
-  L.stage_bytes = plan.stage_bytes;
-  L.poll = tc_poll_;
-  L.hold = tc_hold_;
-  for (size_t c = 0; c < chans_.size(); ++c) {
-    const uint32_t R = chans_[c].nco.rollover;
-    L.nco_base[c] = R ? (uint32_t)(abs0_ % R) : 0u;
-  }
-  int pieces = 0;
-  for (size_t m = 0; m < plan.ms.size(); ++m) {
-    L.ms[m] = plan.ms[m];
-    L.bprefix[m] = pieces;
-    pieces += plan.ms[m].nchunks * 4 * plan.ms[m].NS * 8;
-  }
-  L.bprefix[plan.ms.size()] = pieces;
-  for (size_t s = 0; s < plan.slots.size(); ++s) {
-    L.slots[s] = plan.slots[s];
-    if (plan.slots[s].J > 0)
-      L.slots[s].out = (uint64_t)(uintptr_t)(out[plan.slots[s].ch] + plan.slot_r[s]);
+    FDSP_TRY(cuda_status(cudaMalloc(&d_bbuf_, b_need)));
+    bbuf_cap_ = b_need;
   }
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return FDSP_ERR_UNSUPPORTED;
-  for (size_t g = 0; g < plan.groups.size(); ++g) {
-    const TcPlanGroup& pg = plan.groups[g];
-    L.groups[g].D = pg.D;
-    L.groups[g].S = pg.S;
-    groups_[gmap[g]].tc_split_used = pg.S;
-    // rows of D' samples; a row spans Wx samples (4 16-bit elements each);
-    // (rows - 1) D' + Wx <= xhl_samples keeps every address inside xhl
-    const cuuint64_t rows = (cuuint64_t)((plan.xhl_samples - pg.Wx) / pg.D + 1);
-    const cuuint64_t dims[2] = {(cuuint64_t)(4 * pg.Wx), rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)pg.D * 8u};
-    const cuuint32_t box[2] = {64u, (cuuint32_t)kTcRows};
-    const cuuint32_t estr[2] = {1u, 1u};
-    const CUresult r = enc(&L.maps[g], CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, d_xhl_, dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return FDSP_ERR_UNSUPPORTED;
+  static thread_local TcLaunch L;
+  for (size_t li = 0; li < plans.size(); ++li) {
+    const TcPlan& plan = plans[li];
+    std::memset(&L, 0, sizeof(L));
+    L.block = in16_ ? nullptr : d_in;
+    L.block16 = in16_;
+    L.hist = d_hist_[hist_cur_];
+    L.nco = d_nco_;
+    L.ctaps = d_ctab_;
+    L.xhl = d_xhl_;
+    L.bbuf = d_bbuf_;
+    L.err = d_err_;
+    L.N = (int64_t)n;
+    L.Lc = plan.Lc;
+    L.xhl_n = xhl_need;
+    L.H = H_;
+    L.G = plan.G;
+    L.nmsets = (int32_t)plan.ms.size();
+    L.ngroups = (int32_t)plan.groups.size();
+    L.stages = plan.stages;
+    L.stage_bytes = plan.stage_bytes;
+    L.poll = tc_poll_;
+    L.hold = tc_hold_;
+    for (size_t c = 0; c < chans_.size(); ++c) {
+      const uint32_t R = chans_[c].nco.rollover;
+      L.nco_base[c] = R ? (uint32_t)(abs0_ % R) : 0u;
+    }
+    int pieces = 0;
+    for (size_t m = 0; m < plan.ms.size(); ++m) {
+      L.ms[m] = plan.ms[m];
+      L.bprefix[m] = pieces;
+      pieces += plan.ms[m].nchunks * 4 * plan.ms[m].NS * 8;
+    }
+    L.bprefix[plan.ms.size()] = pieces;
+    for (size_t s = 0; s < plan.slots.size(); ++s) {
+      L.slots[s] = plan.slots[s];
+      if (plan.slots[s].J > 0)
+        L.slots[s].out = (uint64_t)(uintptr_t)(out[plan.slots[s].ch] + plan.slot_r[s]);
+    }
+    for (size_t g = 0; g < plan.groups.size(); ++g) {
+      const TcPlanGroup& pg = plan.groups[g];
+      L.groups[g].D = pg.D;
+      L.groups[g].S = pg.S;
+      groups_[gmap[packs[li][g]]].tc_split_used = pg.S;
+      // rows of D' samples; a row spans Wx samples (4 16-bit elements each);
+      // (rows - 1) D' + Wx <= xhl_samples keeps every address inside xhl
+      const cuuint64_t rows = (cuuint64_t)((plan.xhl_samples - pg.Wx) / pg.D + 1);
+      const cuuint64_t dims[2] = {(cuuint64_t)(4 * pg.Wx), rows};
+      const cuuint64_t strides[1] = {(cuuint64_t)pg.D * 8u};
+      const cuuint32_t box[2] = {64u, (cuuint32_t)kTcRows};
+      const cuuint32_t estr[2] = {1u, 1u};
+      const CUresult r = enc(&L.maps[g], CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, d_xhl_, dims, strides, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return FDSP_ERR_UNSUPPORTED;
+    }
+    // prep: B images (few blocks), then, for the first launch, the split
+    const int nb_build = std::max(1, std::min(num_sms_, (pieces + 255) / 256));
+    const int64_t nb_split = li == 0 ? std::min<int64_t>((xhl_need + 255) / 256, (int64_t)num_sms_ * 8) : 0;
+    auto prep = tc_fmt_ == 0 ? tc_prep_kernel<0> : tc_prep_kernel<1>;
+    prep<<<(unsigned)(nb_build + nb_split), 256, 0, stream>>>(L, nb_build);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+    launches_last_++;
+    auto kern = tc_fmt_ == 0 ? tc_filter_kernel<0> : tc_filter_kernel<1>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, plan.smem);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (kprof_) cudaEventRecord(kprof_event(), stream);
+    kern<<<(unsigned)plan.G, kTcThreads, (size_t)plan.smem, stream>>>(L);
+    if (kprof_) cudaEventRecord(kprof_event(), stream);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+    launches_last_++;
+    tc_groups_last_ += (int)packs[li].size();
   }
-  // prep: B images first (few blocks), then the split
-  const int nb_build = std::max(1, std::min(num_sms_, (pieces + 255) / 256));
-  const int64_t nb_split = std::min<int64_t>((L.xhl_n + 255) / 256, (int64_t)num_sms_ * 8);
-  auto prep = tc_fmt_ == 0 ? tc_prep_kernel<0> : tc_prep_kernel<1>;
-  prep<<<(unsigned)(nb_build + nb_split), 256, 0, stream>>>(L, nb_build);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_status(e);
-  launches_last_++;
-  auto kern = tc_fmt_ == 0 ? tc_filter_kernel<0> : tc_filter_kernel<1>;
-  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, plan.smem);
-  if (e != cudaSuccess) return cuda_status(e);
-  kern<<<(unsigned)plan.G, kTcThreads, (size_t)plan.smem, stream>>>(L);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_status(e);
-  launches_last_++;
-  tc_groups_last_ += (int)gmap.size();
   return FDSP_OK;
 }
 

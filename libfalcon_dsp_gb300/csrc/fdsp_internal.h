@@ -242,6 +242,12 @@ class PolyEngine {
   int tc_error();
   // Polls before a tensor-core wait gives up (each suspends up to ~2 us), and
   // a test hook that makes the next launches' producer issue nothing.
+  // Kernel timing (diagnostics): while on, applies launch directly (no graph)
+  // and every filter-bank launch (tensor-core or FP32) is bracketed by CUDA
+  // events on the apply's stream; read_profile synchronises and returns the
+  // summed milliseconds and the launch count since profiling was enabled.
+  void set_profile(bool on);
+  int read_profile(double* ms, uint32_t* launches);
   void set_tc_wait(uint32_t polls, int hold) {
     tc_poll_ = polls ? polls : 1u;
     tc_hold_ = hold;
@@ -316,6 +322,10 @@ class PolyEngine {
   bool use_tc_for(int eg) const;
   std::vector<cudaEvent_t> prof_ev_;   // autotuning: [2 g] / [2 g + 1] around group g
   std::vector<int> prof_hit_;          // group g launched in the timed apply
+  bool kprof_ = false;                 // kernel timing on
+  std::vector<cudaEvent_t> kprof_ev_;  // (start, end) pairs of the timed launches
+  size_t kprof_used_ = 0;
+  cudaEvent_t kprof_event();           // next free event of the pool
 };
 
 // NCO constants of a (fs, f) pair, following falcon_dsp_freq_shift.cc:194-235.
