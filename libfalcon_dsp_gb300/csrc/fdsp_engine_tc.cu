@@ -236,19 +236,39 @@ __global__ void __launch_bounds__(256) tc_prep_kernel(const __grid_constant__ Tc
 }
 
 // ---------------------------------------------------------------------------
-// NCO rotation of one output (fast path inline, exact path out of line)
+// epilogue constants and the exact NCO path
 // ---------------------------------------------------------------------------
-__device__ __noinline__ float2 tc_rotate_exact(const TcLaunch& L, const TcSlot& S, const NcoConst& nc,
-                                              uint32_t base, int64_t w0, float2 y) {
+// Per-slot epilogue constants, staged in shared memory at CTA start (read
+// with warp-uniform addresses: broadcasts, no constant-cache traffic).
+struct TcEpiSlot {
+  uint64_t out;   // float2*: output of row 0
+  uint64_t om;    // NCO turns per sample (2^-64 units); 0: no rotation
+  int64_t x0;     // NCO counter argument of row 0's window start (base + w0, unreduced)
+  uint32_t R;     // counter rollover; 0: every output takes the exact path
+  int32_t J;      // rows with an output
+  uint32_t U;     // output stride
+  uint32_t Tm1;   // taps - 1
+  int32_t w0;     // window start of row 0 (block relative)
+  int32_t slot;   // index of the slot's launch record
+};
+static_assert(sizeof(TcEpiSlot) == kTcEpiSlotBytes, "epilogue slot table layout");
+
+// Outputs whose window crosses the NCO rollover (or whose counter leaves the
+// fast path's 32-bit range) were stored unrotated; rotate_prep/rotate_apply
+// split the window sum at the rollover exactly, from the FP32 modulated taps.
+__device__ __noinline__ void tc_fix_exact(const TcLaunch& L, int slot, int64_t j, int64_t D, float2* dst) {
+  const TcSlot& S = L.slots[slot];
+  const NcoConst nc = L.nco[S.ch];
   OutMeta cm;
   cm.omega64 = nc.omega64;
   cm.wrap64 = nc.wrap64;
   cm.fastmod = nc.fastmod;
   cm.out = nullptr;
   cm.rollover = nc.rollover;
-  cm.base = base;
+  cm.base = L.nco_base[S.ch];
   cm.enabled = nc.enabled;
   cm.pad_ = 0;
+  const int64_t w0 = (int64_t)S.w0 + j * D;
   const ExactRot er = rotate_prep(cm, w0, S.T);
   float2 B = make_float2(0.f, 0.f);
   if (er.straddle) {
@@ -262,24 +282,7 @@ __device__ __noinline__ float2 tc_rotate_exact(const TcLaunch& L, const TcSlot& 
       B.y = fmaf(gk.y, x.x, B.y);
     }
   }
-  return rotate_apply(er, y, B);
-}
-
-__device__ __forceinline__ float2 tc_rotate(const TcLaunch& L, const TcSlot& S, const NcoConst& nc, uint32_t base,
-                                            int64_t w0, float2 y) {
-  if (!nc.enabled) return y;
-  const int64_t pv = (int64_t)base + w0;
-  const uint32_t R = nc.rollover;
-  uint32_t p;
-  if (pv < 0) {
-    p = (uint32_t)(pv + (int64_t)R);  // w0 > -T > -R
-  } else if (pv < 0x100000000LL) {
-    p = (uint32_t)__umul64hi(nc.fastmod * (uint64_t)(uint32_t)pv, (uint64_t)R);
-  } else {
-    return tc_rotate_exact(L, S, nc, base, w0, y);
-  }
-  if ((uint64_t)p + (uint64_t)S.T - 1 >= (uint64_t)R) return tc_rotate_exact(L, S, nc, base, w0, y);
-  return cmul_nco(y, phasor64_sfu((uint64_t)p * nc.omega64));
+  *dst = rotate_apply(er, *dst, B);
 }
 
 // ---------------------------------------------------------------------------
@@ -316,6 +319,37 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
     }
     tc::mbar_init(&drain_bar, 1);
     tc::mbar_fence_init();
+  }
+  // epilogue constants of every slot of the launch (after the stages)
+  TcEpiSlot* etab =
+      reinterpret_cast<TcEpiSlot*>(smem_raw + (sbase - tc::smem_u32(smem_raw)) + (size_t)stages * L.stage_bytes);
+  for (int s = tid; s < L.nslots; s += kTcThreads) {
+    const TcSlot& S = L.slots[s];
+    int64_t D = 2;
+    for (int m = 0; m < L.nmsets; ++m)
+      if (s >= L.ms[m].slot0 && s < L.ms[m].slot0 + L.ms[m].NS) D = L.groups[L.ms[m].group].D;
+    TcEpiSlot e;
+    e.out = S.out;
+    e.J = S.J;
+    e.U = S.U;
+    e.w0 = S.w0;
+    e.slot = s;
+    e.Tm1 = S.T > 0 ? (uint32_t)S.T - 1u : 0u;
+    e.om = 0;
+    e.x0 = 0;
+    e.R = 0xFFFFFFFFu;
+    if (S.J > 0) {
+      const NcoConst nc = L.nco[S.ch];
+      if (nc.enabled) {
+        // fast path: row counters (P0 + lane D) stay below 2 R < 2^32 with one
+        // conditional subtraction; otherwise every output goes exact (R = 0)
+        const bool fast = nc.rollover < 0x80000000u && (int64_t)31 * D + S.T < (int64_t)nc.rollover;
+        e.om = nc.omega64;
+        e.x0 = (int64_t)L.nco_base[S.ch] + S.w0;
+        e.R = fast ? nc.rollover : 0u;
+      }
+    }
+    etab[s] = e;
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -451,25 +485,53 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
       const TcMset& M = L.ms[m];
       const int R = M.R, NS = M.NS, nch = NS >> 3;
       const int64_t D = L.groups[M.group].D;
+      const uint32_t laneD = (uint32_t)lane * (uint32_t)D;
       for (int idx = h; idx < R * nch; idx += 2) {
         const int r = idx / nch, cc = idx - r * nch;
-        const int64_t j = ((int64_t)t * R + r) * kTcRows + q * 32 + lane;
+        const int64_t row0 = ((int64_t)t * R + r) * kTcRows + q * 32;  // row of lane 0
+        const int64_t j = row0 + lane;
         const uint32_t col = tbase + lane_off + (uint32_t)a * 256u + (uint32_t)(r * (256 / R) + 16 * cc);
         uint32_t vh[16], vl[16];
         tc::tmem_ld16(col, vh);
         tc::tmem_ld16(col + (uint32_t)(2 * NS), vl);
+        const TcEpiSlot* E8 = etab + M.slot0 + cc * 8;
+        // NCO counter of lane 0's window start for slot e (lane e computes it):
+        // (x0 + row0 D) mod R, reduced once per chunk
+        uint32_t p0 = 0;
+        if (lane < 8) {
+          const TcEpiSlot& E = E8[lane];
+          if (E.om != 0 && E.R != 0) {
+            const int64_t v = E.x0 + row0 * D;
+            p0 = v < 0 ? (uint32_t)(v + (int64_t)E.R) : (uint32_t)((uint64_t)v % E.R);
+          }
+        }
         tc::tmem_wait_ld();
+        uint32_t slow = 0;
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
-          const TcSlot& S = L.slots[M.slot0 + cc * 8 + e];
-          if (j < S.J) {
-            const float2 y0 = make_float2(__uint_as_float(vh[2 * e]) + __uint_as_float(vl[2 * e]),
-                                          __uint_as_float(vh[2 * e + 1]) + __uint_as_float(vl[2 * e + 1]));
-            const NcoConst nc = L.nco[S.ch];
-            const float2 y = tc_rotate(L, S, nc, L.nco_base[S.ch], (int64_t)S.w0 + j * D, y0);
-            float2* dst = reinterpret_cast<float2*>(S.out) + (uint64_t)S.U * (uint64_t)j;
-            __stcs(dst, y);
+          const TcEpiSlot& E = E8[e];
+          const uint32_t P0 = __shfl_sync(0xffffffffu, p0, e);
+          const float2 y0 = make_float2(__uint_as_float(vh[2 * e]) + __uint_as_float(vl[2 * e]),
+                                        __uint_as_float(vh[2 * e + 1]) + __uint_as_float(vl[2 * e + 1]));
+          uint32_t pc = P0 + laneD;
+          pc = pc >= E.R ? pc - E.R : pc;
+          const bool fast = pc + E.Tm1 < E.R || E.om == 0;
+          const uint32_t om_lo = (uint32_t)E.om, om_hi = (uint32_t)(E.om >> 32);
+          const uint32_t turns = __umulhi(pc, om_lo) + pc * om_hi;  // bits 32..63 of pc * om: 2^-32 turns
+          float sn, cs;
+          __sincosf((float)(int32_t)turns * 1.4629180792671596e-09f, &sn, &cs);  // 2 pi / 2^32
+          const float2 y = cmul_nco(y0, make_float2(cs, sn));
+          if (j < E.J) {
+            float2* dst = reinterpret_cast<float2*>(E.out) + (uint64_t)E.U * (uint64_t)j;
+            __stcs(dst, fast ? y : y0);
+            slow |= fast ? 0u : (1u << e);
           }
+        }
+        while (slow) {  // rare: windows across the NCO rollover
+          const int e = __ffs(slow) - 1;
+          slow &= slow - 1;
+          const TcEpiSlot& E = E8[e];
+          tc_fix_exact(L, E.slot, j, D, reinterpret_cast<float2*>(E.out) + (uint64_t)E.U * (uint64_t)j);
         }
       }
       tc::fence_before_sync();
@@ -710,6 +772,7 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     L.ngroups = (int32_t)plan.groups.size();
     L.stages = plan.stages;
     L.stage_bytes = plan.stage_bytes;
+    L.nslots = (int32_t)plan.slots.size();
     L.poll = tc_poll_;
     L.hold = tc_hold_;
     for (size_t c = 0; c < chans_.size(); ++c) {

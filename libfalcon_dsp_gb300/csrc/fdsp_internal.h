@@ -116,7 +116,7 @@ struct TcLaunch {
   int64_t N;                         // block samples
   int64_t Lc;                        // samples of the time range each CTA owns
   int64_t xhl_n;                     // samples of xhl the prep writes
-  int32_t H, G, nmsets, ngroups, stages, stage_bytes;
+  int32_t H, G, nmsets, ngroups, stages, stage_bytes, nslots;
   uint32_t poll;                     // polls before a wait gives up (each suspends up to ~2 us)
   int32_t hold;                      // test hook: the producer issues nothing (every wait runs out)
   int32_t bprefix[kTcMaxMsets + 1];  // 16-byte pieces of the B images before merge set m

@@ -52,6 +52,7 @@ constexpr int kTcMsetSlots = 32;       // slots per merge set (N = 4 NS <= 128)
 constexpr int kTcStageMaxBytes = 49152;
 constexpr int kTcSmemDyn = 225 * 1024; // dynamic shared memory ceiling (227 KB minus static and alignment)
 constexpr int kTcMaxStages = 6;
+constexpr int kTcEpiSlotBytes = 48;    // per-slot epilogue constants staged in shared memory
 
 // ---- launch records (kernel parameters; shared with the device code) -----
 struct TcGroup {
@@ -106,7 +107,7 @@ struct TcPlan {
   std::vector<int> slot_r;        // output offset r of each slot (for the out pointer)
   size_t b_bytes = 0;
   int64_t xhl_samples = 0;        // [history | block | zero pad] samples the split writes
-  int stages = 0, stage_bytes = 0, smem = 0;
+  int stages = 0, stage_bytes = 0, smem = 0;  // smem: stages, then the epilogue slot table
   int G = 0;                      // grid (CTAs)
   int64_t Lc = 0;                 // samples of the time range each CTA owns
   int64_t items = 0;
@@ -239,9 +240,10 @@ inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_
     sb = std::max<int>(sb, m.R * kTcTileBytes + (int)tc_round_up((int64_t)4 * m.NS * 128, 1024));
   if (sb > kTcStageMaxBytes) return -1;
   p.stage_bytes = sb;
-  p.stages = std::min(kTcMaxStages, (kTcSmemDyn - 1024) / sb);
+  const int table = (int)tc_round_up((int64_t)p.slots.size() * kTcEpiSlotBytes, 1024);
+  p.stages = std::min(kTcMaxStages, (kTcSmemDyn - 1024 - table) / sb);
   if (p.stages < 2) return -1;
-  p.smem = p.stages * sb + 1024;
+  p.smem = p.stages * sb + table + 1024;
   // schedule: each CTA owns a contiguous range of input samples and runs the
   // items of every merge set that start in it, in input order
   int64_t umax = 0;

@@ -131,6 +131,8 @@ int main(int argc, char** argv) {
           "record limits");
     if (p.ms.empty()) continue;
     CHECK(p.smem <= kTcSmemDyn && p.stages >= 2 && p.stages <= kTcMaxStages, "smem %d stages %d", p.smem, p.stages);
+    CHECK((int64_t)p.stages * p.stage_bytes + (int64_t)p.slots.size() * kTcEpiSlotBytes + 1024 <= p.smem,
+          "stages + epilogue table inside the dynamic shared memory");
     CHECK(p.xhl_samples >= N + H, "split buffer");
     // coverage: one writer per output
     std::vector<std::vector<uint8_t>> hit(nch);
