@@ -53,8 +53,9 @@
 
 namespace fdsp {
 
-constexpr int kTcThreads = 320;
-constexpr int kTcEpiWarps = 8;
+constexpr int kTcEpiWarps = 16;                       // four per TMEM lane quarter
+constexpr int kTcThreads = 64 + 32 * kTcEpiWarps;     // producer warp, MMA warp, epilogue warps
+constexpr int kTcRing = 16;                           // items announced ahead (> stages + 2)
 constexpr uint32_t kTmemCols = 512;
 
 // ---------------------------------------------------------------------------
@@ -129,16 +130,17 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
-// The sequence of items (merge set, item index) a CTA runs: every role walks
-// it the same way.  Items of merge set m start at input sample a + t P.
+// The sequence of items (merge set, item index) a CTA runs, walked by the
+// producer alone (its arrays in shared memory: local memory would miss L1,
+// which the stages leave small) and announced to the MMA and epilogue warps
+// through a ring of (merge set, item) entries.  Items of merge set m start at
+// input sample a + t P; the next item is the earliest start.
 struct TcCursor {
   int32_t cur[kTcMaxMsets];
   int32_t end[kTcMaxMsets];
   int64_t P[kTcMaxMsets];
-  int n;
   __device__ void init(const TcLaunch& L, int b) {
-    n = L.nmsets;
-    for (int m = 0; m < n; ++m) {
+    for (int m = 0; m < L.nmsets; ++m) {
       const TcMset& M = L.ms[m];
       P[m] = (int64_t)M.R * kTcRows * L.groups[M.group].D;
       int64_t f, l;
@@ -150,7 +152,7 @@ struct TcCursor {
   __device__ bool next(const TcLaunch& L, int* m_out, int* t_out) {
     int best = -1;
     int64_t bu = 0;
-    for (int m = 0; m < n; ++m) {
+    for (int m = 0; m < L.nmsets; ++m) {
       if (cur[m] >= end[m]) continue;
       const int64_t u = (int64_t)L.ms[m].a + (int64_t)cur[m] * P[m];
       if (best < 0 || u < bu) {
@@ -243,13 +245,14 @@ __global__ void __launch_bounds__(256) tc_prep_kernel(const __grid_constant__ Tc
 struct TcEpiSlot {
   uint64_t out;   // float2*: output of row 0
   uint64_t om;    // NCO turns per sample (2^-64 units); 0: no rotation
+  uint64_t fm;    // ceil(2^64 / R): (a mod R) as one multiply-high (Lemire et al. 2019)
   int64_t x0;     // NCO counter argument of row 0's window start (base + w0, unreduced)
   uint32_t R;     // counter rollover; 0: every output takes the exact path
   int32_t J;      // rows with an output
   uint32_t U;     // output stride
   uint32_t Tm1;   // taps - 1
-  int32_t w0;     // window start of row 0 (block relative)
   int32_t slot;   // index of the slot's launch record
+  int32_t pad_[3];
 };
 static_assert(sizeof(TcEpiSlot) == kTcEpiSlotBytes, "epilogue slot table layout");
 
@@ -297,6 +300,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   __shared__ __align__(8) uint64_t acc_empty[2];
   __shared__ __align__(8) uint64_t drain_bar;
   __shared__ uint32_t tmem_base_s;
+  __shared__ int2 ring[kTcRing];       // item k: (merge set, item index); merge set -1 ends the sequence
+  __shared__ TcCursor cursor;
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
@@ -332,10 +337,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
     e.out = S.out;
     e.J = S.J;
     e.U = S.U;
-    e.w0 = S.w0;
     e.slot = s;
+    e.pad_[0] = e.pad_[1] = e.pad_[2] = 0;
     e.Tm1 = S.T > 0 ? (uint32_t)S.T - 1u : 0u;
     e.om = 0;
+    e.fm = 0;
     e.x0 = 0;
     e.R = 0xFFFFFFFFu;
     if (S.J > 0) {
@@ -345,6 +351,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
         // conditional subtraction; otherwise every output goes exact (R = 0)
         const bool fast = nc.rollover < 0x80000000u && (int64_t)31 * D + S.T < (int64_t)nc.rollover;
         e.om = nc.omega64;
+        e.fm = nc.fastmod;
         e.x0 = (int64_t)L.nco_base[S.ch] + S.w0;
         e.R = fast ? nc.rollover : 0u;
       }
@@ -359,12 +366,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
-      TcCursor cur;
+      TcCursor& cur = cursor;
       cur.init(L, blockIdx.x);
       int64_t ci = 0;  // chunks issued
+      int64_t k = 0;   // items announced
       bool failed = false;
       int m, t;
-      while (!L.hold && !failed && cur.next(L, &m, &t)) {
+      while (!L.hold && !failed) {
+        const bool more = cur.next(L, &m, &t);
+        // announce item k (or the end of the sequence) with its first stage
+        {
+          const int s = (int)(ci % stages);
+          const int64_t kk = ci / stages;
+          if (kk > 0 && !tc::mbar_wait_bounded(&empty_bar[s], (uint32_t)((kk - 1) & 1), poll)) {
+            failed = true;
+            break;
+          }
+          ring[k % kTcRing] = make_int2(more ? m : -1, more ? t : 0);
+          ++k;
+          if (!more) {
+            tc::mbar_arrive(&full_bar[s]);  // no copies: the consumers read the end marker
+            ++ci;
+            break;
+          }
+        }
         const TcMset& M = L.ms[m];
         const int D = L.groups[M.group].D;
         const CUtensorMap* map = &L.maps[M.group];
@@ -376,8 +401,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
         const uint8_t* bsrc = L.bbuf + M.b;
         for (int c = 0; c < M.nchunks; ++c, ++ci) {
           const int s = (int)(ci % stages);
-          const int64_t k = ci / stages;
-          if (k > 0 && !tc::mbar_wait_bounded(&empty_bar[s], (uint32_t)((k - 1) & 1), poll)) {
+          const int64_t kk = ci / stages;
+          // (the first chunk's stage was claimed with the announcement)
+          if (c > 0 && kk > 0 && !tc::mbar_wait_bounded(&empty_bar[s], (uint32_t)((kk - 1) & 1), poll)) {
             failed = true;
             break;
           }
@@ -395,41 +421,43 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
-    TcCursor cur;
-    if (lane == 0) cur.init(L, blockIdx.x);
     int64_t ci = 0;
     int k = 0;
     bool failed = false, issued = false;
-    int m = 0, t = 0;
+    // every wait is taken by lane 0 and its outcome shared with the warp
+    auto wait_warp = [&](uint64_t* bar, uint32_t parity) {
+      bool ok = true;
+      if (lane == 0) ok = tc::mbar_wait_bounded(bar, parity, poll);
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      tc::fence_after_sync();
+      return ok;
+    };
     while (true) {
-      int have = 0;
-      if (lane == 0) have = cur.next(L, &m, &t) ? 1 : 0;
-      have = __shfl_sync(0xffffffffu, have, 0);
-      if (!have) break;
-      m = __shfl_sync(0xffffffffu, m, 0);
-      const TcMset& M = L.ms[m];
-      const int a = k & 1;
-      if (k >= 2) {
-        bool ok = true;
-        if (lane == 0) ok = tc::mbar_wait_bounded(&acc_empty[a], (uint32_t)(((k >> 1) - 1) & 1), poll);
-        if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
-          failed = true;
-          break;
-        }
-        tc::fence_after_sync();
+      // the first stage of item k also announces it (ring entry k)
+      if (!wait_warp(&full_bar[ci % stages], (uint32_t)((ci / stages) & 1))) {
+        failed = true;
+        break;
       }
+      const int2 it = ring[k % kTcRing];
+      const int a = k & 1;
+      if (k >= 2 && !wait_warp(&acc_empty[a], (uint32_t)(((k >> 1) - 1) & 1))) {
+        failed = true;
+        break;
+      }
+      if (it.x < 0) {  // end of the sequence: pass it on through the accumulator slot
+        if (lane == 0) tc::mbar_arrive(&acc_full[a]);
+        break;
+      }
+      const TcMset& M = L.ms[it.x];
       const int R = M.R, N = 4 * M.NS;
       const uint32_t idesc = tc::idesc_f16(FMT, 128, (uint32_t)N);
       const uint32_t dcol = tbase + (uint32_t)a * 256u;
-      for (int c = 0; c < M.nchunks && !failed; ++c, ++ci) {
+      for (int c = 0; c < M.nchunks; ++c, ++ci) {
         const int s = (int)(ci % stages);
-        bool ok = true;
-        if (lane == 0) ok = tc::mbar_wait_bounded(&full_bar[s], (uint32_t)((ci / stages) & 1), poll);
-        if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
+        if (c > 0 && !wait_warp(&full_bar[s], (uint32_t)((ci / stages) & 1))) {
           failed = true;
           break;
         }
-        tc::fence_after_sync();
         if (lane == 0) {
           const uint32_t st = sbase + (uint32_t)s * (uint32_t)L.stage_bytes;
           const uint64_t bdesc = desc_sw128(st + (uint32_t)R * kTcTileBytes);
@@ -461,19 +489,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   } else {
     // ------------------------------------------------------------ epilogue
     const int q = warp & 3;           // TMEM lane quarter this warp may read
-    const int h = (warp - 2) >> 2;    // which of the item's column chunks
+    const int h = (warp - 2) >> 2;    // which of the item's column chunks (every fourth)
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-    TcCursor cur;
-    if (lane == 0) cur.init(L, blockIdx.x);
     bool failed = false;
-    int k = 0, m = 0, t = 0;
-    while (true) {
-      int have = 0;
-      if (lane == 0) have = cur.next(L, &m, &t) ? 1 : 0;
-      have = __shfl_sync(0xffffffffu, have, 0);
-      if (!have) break;
-      m = __shfl_sync(0xffffffffu, m, 0);
-      t = __shfl_sync(0xffffffffu, t, 0);
+    for (int k = 0;; ++k) {
       const int a = k & 1;
       bool ok = true;
       if (lane == 0) ok = tc::mbar_wait_bounded(&acc_full[a], (uint32_t)((k >> 1) & 1), poll);
@@ -482,11 +501,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
         break;
       }
       tc::fence_after_sync();
+      const int2 it = ring[k % kTcRing];
+      if (it.x < 0) break;
+      const int m = it.x, t = it.y;
       const TcMset& M = L.ms[m];
       const int R = M.R, NS = M.NS, nch = NS >> 3;
       const int64_t D = L.groups[M.group].D;
       const uint32_t laneD = (uint32_t)lane * (uint32_t)D;
-      for (int idx = h; idx < R * nch; idx += 2) {
+      for (int idx = h; idx < R * nch; idx += 4) {
         const int r = idx / nch, cc = idx - r * nch;
         const int64_t row0 = ((int64_t)t * R + r) * kTcRows + q * 32;  // row of lane 0
         const int64_t j = row0 + lane;
@@ -496,13 +518,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
         tc::tmem_ld16(col + (uint32_t)(2 * NS), vl);
         const TcEpiSlot* E8 = etab + M.slot0 + cc * 8;
         // NCO counter of lane 0's window start for slot e (lane e computes it):
-        // (x0 + row0 D) mod R, reduced once per chunk
+        // (x0 + row0 D) mod R, once per chunk; 0 <= x0 + row0 D < 2^32 or
+        // > -R on the fast path
         uint32_t p0 = 0;
         if (lane < 8) {
           const TcEpiSlot& E = E8[lane];
           if (E.om != 0 && E.R != 0) {
             const int64_t v = E.x0 + row0 * D;
-            p0 = v < 0 ? (uint32_t)(v + (int64_t)E.R) : (uint32_t)((uint64_t)v % E.R);
+            p0 = v < 0 ? (uint32_t)(v + (int64_t)E.R)
+                       : (uint32_t)__umul64hi(E.fm * (uint64_t)(uint32_t)v, (uint64_t)E.R);
           }
         }
         tc::tmem_wait_ld();
@@ -537,7 +561,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acc_empty[a]);
-      ++k;
     }
     if (failed && lane == 0) atomicExch(L.err, 1);
   }
