@@ -20,9 +20,9 @@
 // A row split S (rows j = S i + b become S slots whose rows are S D apart)
 // widens groups with few slots, and makes an odd D even (TMA strides are
 // multiples of 16 bytes = 2 samples).  Slots sorted by window start are
-// merged greedily into merge sets ("msets") of <= 32 slots whose windows
-// span at most cap(T) taps; an mset's window starts on an even sample (TMA
-// x coordinates are multiples of 16 bytes) and is chunked in 16 taps.
+// partitioned into merge sets ("msets") of <= 64 slots (N <= 256) by the
+// fewest K chunks; an mset's window starts on an even sample (TMA x
+// coordinates are multiples of 16 bytes) and is chunked in 16 taps.
 //
 // Kept apart from the kernel so that its bounds can be checked on the CPU
 // (tests/cpp/tc_plan_check.cc).
@@ -48,7 +48,7 @@ constexpr int kTcMaxSlots = 512;
 constexpr int kTcRows = 128;           // rows per tile (MMA M)
 constexpr int kTcChunkTaps = 16;       // taps per K chunk: 128 bytes of A per row
 constexpr int kTcTileBytes = kTcRows * 128;
-constexpr int kTcMsetSlots = 32;       // slots per merge set (N = 4 NS <= 128)
+constexpr int kTcMsetSlots = 64;       // slots per merge set (N = 4 NS <= 256)
 constexpr int kTcStageMaxBytes = 49152;
 constexpr int kTcSmemDyn = 225 * 1024; // dynamic shared memory ceiling (227 KB minus static and alignment)
 constexpr int kTcMaxStages = 6;
@@ -115,20 +115,98 @@ struct TcPlan {
 
 inline int64_t tc_round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
-// Window span a merge set may reach for its longest filter T: a quarter more
-// than T, at least T + 17 (padding slots' windows to one chunk costs less
-// than one more merge set).
-inline int64_t tc_window_cap(int64_t T) { return T + std::max<int64_t>(17, T / 4); }
+// A slot of a split group: output m = r + U j, window ending at delta + j D'.
+struct TcSlotX {
+  TcSlotIn s;
+  int64_t start;  // window start of row 0 (block relative)
+};
 
-// Row split of a group: odd D needs S even; beyond that the split doubles
-// while the slots still fill at most one merge set and the windows of the
-// split rows stay within the cap of the longest filter.
-inline int tc_choose_split(int D, int nslots, int Tmax, int max_split) {
-  int S = (D & 1) ? 2 : 1;
-  while (S * 2 <= max_split && (int64_t)nslots * S * 2 <= kTcMsetSlots &&
-         (int64_t)(2 * S - 1) * D <= tc_window_cap(Tmax) - Tmax)
-    S *= 2;
-  return S;
+// The group's slots under row split S, sorted by window start.
+inline std::vector<TcSlotX> tc_split_slots(const TcGroupIn& g, int S) {
+  std::vector<TcSlotX> xs;
+  for (const TcSlotIn& s : g.slots) {
+    for (int b = 0; b < S; ++b) {
+      if (s.J <= b) continue;
+      TcSlotX x;
+      x.s = s;
+      x.s.delta = s.delta + (int64_t)b * g.D;
+      x.s.J = (s.J - b + S - 1) / S;
+      x.s.U = s.U * S;
+      x.s.r = s.r + b * s.U;
+      x.start = x.s.delta - s.T + 1;
+      xs.push_back(x);
+    }
+  }
+  std::stable_sort(xs.begin(), xs.end(), [](const TcSlotX& a, const TcSlotX& b) {
+    return a.start != b.start ? a.start < b.start : a.s.delta < b.s.delta;
+  });
+  return xs;
+}
+
+// Merge-set window of slots [i, j) (sorted by start): its start in
+// [history | block] samples rounded down to even, and its K chunks.
+inline void tc_window(const std::vector<TcSlotX>& xs, size_t i, size_t j, int H, int64_t* a, int64_t* chunks) {
+  int64_t st = xs[i].start + H;
+  if (st & 1) st -= 1;
+  int64_t end = xs[i].s.delta;
+  for (size_t q = i + 1; q < j; ++q) end = std::max(end, xs[q].s.delta);
+  *a = st;
+  *chunks = (end + H - st + 1 + kTcChunkTaps - 1) / kTcChunkTaps;
+}
+
+// Partition of the sorted slots into merge sets of at most kTcMsetSlots
+// slots minimising the total K chunks: one MMA of M = 128, K = 16 costs the
+// same for any N up to 256, so the work of a tile is its merge sets' chunks
+// (dynamic programming over the split points).  Returns the cut points and
+// the chunks per tile row.
+inline int64_t tc_partition(const std::vector<TcSlotX>& xs, int H, std::vector<size_t>& cuts) {
+  const size_t n = xs.size();
+  std::vector<int64_t> best(n + 1, INT64_MAX);
+  std::vector<size_t> from(n + 1, 0);
+  best[0] = 0;
+  for (size_t i = 0; i < n; ++i) {
+    if (best[i] == INT64_MAX) continue;
+    int64_t st = xs[i].start + H;
+    if (st & 1) st -= 1;
+    int64_t end = xs[i].s.delta;
+    for (size_t j = i + 1; j <= n && (int)(j - i) <= kTcMsetSlots; ++j) {
+      end = std::max(end, xs[j - 1].s.delta);
+      const int64_t c = best[i] + (end + H - st + 1 + kTcChunkTaps - 1) / kTcChunkTaps;
+      if (c < best[j]) {
+        best[j] = c;
+        from[j] = i;
+      }
+    }
+  }
+  cuts.clear();
+  for (size_t j = n; j > 0; j = from[j]) cuts.push_back(j);
+  cuts.push_back(0);
+  std::reverse(cuts.begin(), cuts.end());
+  return best[n];
+}
+
+// Row split of a group: the power of two up to max_split (S even for odd D,
+// so that rows start 16 bytes apart) with the fewest K chunks over all its
+// tiles (chunks per tile row x rows / S); ties keep the smaller split.  The
+// split slots stay within four full merge sets.
+inline int tc_choose_split(const TcGroupIn& g, int H) {
+  int64_t J = 0;
+  for (const TcSlotIn& s : g.slots) J = std::max(J, s.J);
+  int bestS = 0;
+  double bestc = 0;
+  for (int S = 1; S <= std::max(1, g.max_split); S *= 2) {
+    if ((g.D & 1) && (S & 1)) continue;
+    if (S > 2 && (int64_t)g.slots.size() * S > 4 * kTcMsetSlots) break;
+    const std::vector<TcSlotX> xs = tc_split_slots(g, S);
+    if (xs.empty()) continue;
+    std::vector<size_t> cuts;
+    const double c = (double)tc_partition(xs, H, cuts) * (double)((J + (int64_t)S * kTcRows - 1) / ((int64_t)S * kTcRows));
+    if (bestS == 0 || c < bestc) {
+      bestS = S;
+      bestc = c;
+    }
+  }
+  return bestS == 0 ? ((g.D & 1) ? 2 : 1) : bestS;
 }
 
 // Returns 0 on success, -1 when the apply exceeds a launch's record limits
@@ -138,59 +216,27 @@ inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_
   int64_t wx_max = 0;
   for (const TcGroupIn& g : gin) {
     if (g.slots.empty()) continue;
-    int Tmax = 1;
-    for (const TcSlotIn& s : g.slots) Tmax = std::max(Tmax, s.T);
-    const int S = tc_choose_split(g.D, (int)g.slots.size(), Tmax, std::max(1, g.max_split));
+    const int S = tc_choose_split(g, H);
     const int64_t Dp = (int64_t)S * g.D;
-    // slots of the split rows
-    struct X {
-      TcSlotIn s;
-      int64_t start;  // window start of row 0 (block relative)
-    };
-    std::vector<X> xs;
-    for (const TcSlotIn& s : g.slots) {
-      for (int b = 0; b < S; ++b) {
-        if (s.J <= b) continue;
-        X x;
-        x.s = s;
-        x.s.delta = s.delta + (int64_t)b * g.D;
-        x.s.J = (s.J - b + S - 1) / S;
-        x.s.U = s.U * S;
-        x.s.r = s.r + b * s.U;
-        x.start = x.s.delta - s.T + 1;
-        xs.push_back(x);
-      }
-    }
+    const std::vector<TcSlotX> xs = tc_split_slots(g, S);
     if (xs.empty()) continue;
-    std::stable_sort(xs.begin(), xs.end(), [](const X& a, const X& b) {
-      return a.start != b.start ? a.start < b.start : a.s.delta < b.s.delta;
-    });
     if ((int)p.groups.size() >= kTcMaxGroups) return -1;
     const int gi = (int)p.groups.size();
     TcPlanGroup pg;
     pg.D = (int)Dp;
     pg.S = S;
     pg.Wx = 0;
-    size_t i = 0;
-    while (i < xs.size()) {
-      // window start of the merge set in [history | block] samples, even
-      int64_t a = xs[i].start + H;
-      if (a & 1) a -= 1;
-      int64_t end = xs[i].s.delta, tm = xs[i].s.T;
-      size_t j = i + 1;
-      while (j < xs.size() && (int)(j - i) < kTcMsetSlots) {
-        const int64_t e2 = std::max(end, xs[j].s.delta), t2 = std::max<int64_t>(tm, xs[j].s.T);
-        if (e2 + H - a + 1 > tc_window_cap(t2)) break;
-        end = e2;
-        tm = t2;
-        ++j;
-      }
-      const int64_t Kw = end + H - a + 1;
+    std::vector<size_t> cuts;
+    tc_partition(xs, H, cuts);
+    for (size_t ci = 0; ci + 1 < cuts.size(); ++ci) {
+      const size_t i = cuts[ci], j = cuts[ci + 1];
+      int64_t a, nchunks;
+      tc_window(xs, i, j, H, &a, &nchunks);
       const int nreal = (int)(j - i);
       // record field ranges (16-bit taps, strides and offsets)
-      if (Kw > 65535 || tm > 65535) return -1;
+      if (nchunks * kTcChunkTaps > 65535) return -1;
       for (size_t q = i; q < j; ++q)
-        if (xs[q].s.U > 65535 || xs[q].s.phi > 65535 || xs[q].s.J > INT32_MAX) return -1;
+        if (xs[q].s.T > 65535 || xs[q].s.U > 65535 || xs[q].s.phi > 65535 || xs[q].s.J > INT32_MAX) return -1;
       const int NS = (int)tc_round_up(nreal, 8);
       if ((int)p.ms.size() >= kTcMaxMsets || (int)p.slots.size() + NS > kTcMaxSlots) return -1;
       TcMset m{};
@@ -198,11 +244,11 @@ inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_
       m.group = (int16_t)gi;
       m.slot0 = (int16_t)p.slots.size();
       m.NS = (int16_t)NS;
-      m.nchunks = (int16_t)((Kw + kTcChunkTaps - 1) / kTcChunkTaps);
+      m.nchunks = (int16_t)nchunks;
       m.R = (int16_t)(4 * NS <= 128 ? 2 : 1);
       int64_t Jmax = 0;
       for (size_t q = i; q < j; ++q) {
-        const X& x = xs[q];
+        const TcSlotX& x = xs[q];
         TcSlot s{};
         s.w0 = (int32_t)x.start;
         s.J = (int32_t)x.s.J;
@@ -225,7 +271,6 @@ inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_
       p.b_bytes += (size_t)tc_round_up((int64_t)m.nchunks * 4 * NS * 128, 1024);
       pg.Wx = std::max<int64_t>(pg.Wx, a % Dp + (int64_t)m.nchunks * kTcChunkTaps);
       p.ms.push_back(m);
-      i = j;
     }
     wx_max = std::max(wx_max, pg.Wx);
     p.groups.push_back(pg);
