@@ -252,7 +252,8 @@ struct TcEpiSlot {
   uint32_t U;     // output stride
   uint32_t Tm1;   // taps - 1
   int32_t slot;   // index of the slot's launch record
-  int32_t pad_[3];
+  uint32_t pair;  // 1: the next slot holds this channel's next output (one 16-byte store)
+  int32_t pad_[2];
 };
 static_assert(sizeof(TcEpiSlot) == kTcEpiSlotBytes, "epilogue slot table layout");
 
@@ -338,7 +339,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
     e.J = S.J;
     e.U = S.U;
     e.slot = s;
-    e.pad_[0] = e.pad_[1] = e.pad_[2] = 0;
+    e.pair = S.flags & 1u;
+    e.pad_[0] = e.pad_[1] = 0;
     e.Tm1 = S.T > 0 ? (uint32_t)S.T - 1u : 0u;
     e.om = 0;
     e.fm = 0;
@@ -531,6 +533,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
         }
         tc::tmem_wait_ld();
         uint32_t slow = 0;
+        float2 o[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
           const TcEpiSlot& E = E8[e];
@@ -545,10 +548,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
           float sn, cs;
           __sincosf((float)(int32_t)turns * 1.4629180792671596e-09f, &sn, &cs);  // 2 pi / 2^32
           const float2 y = cmul_nco(y0, make_float2(cs, sn));
-          if (j < E.J) {
-            float2* dst = reinterpret_cast<float2*>(E.out) + (uint64_t)E.U * (uint64_t)j;
-            __stcs(dst, fast ? y : y0);
-            slow |= fast ? 0u : (1u << e);
+          o[e] = fast ? y : y0;
+          slow |= (fast || j >= E.J) ? 0u : (1u << e);
+        }
+        // stores: a slot and the next one holding the same channel's next
+        // output go out as one 16-byte store (contiguous across the lanes
+        // when the channel's outputs interleave by two)
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          const TcEpiSlot& E0 = E8[e];
+          const TcEpiSlot& E1 = E8[e + 1];
+          float2* d0 = reinterpret_cast<float2*>(E0.out) + (uint64_t)E0.U * (uint64_t)j;
+          const bool v0 = j < E0.J, v1 = j < E1.J;
+          if (E0.pair && v0 && v1 && (reinterpret_cast<uintptr_t>(d0) & 15u) == 0) {
+            __stcs(reinterpret_cast<float4*>(d0), make_float4(o[e].x, o[e].y, o[e + 1].x, o[e + 1].y));
+          } else {
+            if (v0) __stcs(d0, o[e]);
+            if (v1) __stcs(reinterpret_cast<float2*>(E1.out) + (uint64_t)E1.U * (uint64_t)j, o[e + 1]);
           }
         }
         while (slow) {  // rare: windows across the NCO rollover

@@ -20,9 +20,10 @@
 // A row split S (rows j = S i + b become S slots whose rows are S D apart)
 // widens groups with few slots, and makes an odd D even (TMA strides are
 // multiples of 16 bytes = 2 samples).  Slots sorted by window start are
-// partitioned into merge sets ("msets") of <= 64 slots (N <= 256) by the
-// fewest K chunks; an mset's window starts on an even sample (TMA x
-// coordinates are multiples of 16 bytes) and is chunked in 16 taps.
+// kept together per channel (a bundle, in output order) and partitioned into
+// merge sets ("msets") of <= 64 slots (N <= 256) by the fewest K chunks; an
+// mset's window starts on an even sample (TMA x coordinates are multiples of
+// 16 bytes) and is chunked in 16 taps.
 //
 // Kept apart from the kernel so that its bounds can be checked on the CPU
 // (tests/cpp/tc_plan_check.cc).
@@ -32,6 +33,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <vector>
 
 #if defined(__CUDACC__)
@@ -78,7 +80,8 @@ struct TcSlot {
   uint16_t U;       // output stride (up rate x row split)
   uint16_t o;       // window start inside the merge set's window (taps)
   uint16_t phi;     // tap phase
-  uint16_t pad_[3];
+  uint16_t flags;   // bit 0: the next slot holds the same channel's next output (pair store)
+  uint16_t pad_[2];
 };
 static_assert(sizeof(TcSlot) == 32, "slot record");
 static_assert(sizeof(TcMset) == 32, "merge-set record");
@@ -121,8 +124,19 @@ struct TcSlotX {
   int64_t start;  // window start of row 0 (block relative)
 };
 
-// The group's slots under row split S, sorted by window start.
-inline std::vector<TcSlotX> tc_split_slots(const TcGroupIn& g, int S) {
+// A bundle: every slot of one channel under row split S, in output order
+// (offset r + b U = 0 .. U S - 1), so that row j of the bundle holds the
+// channel's consecutive outputs U S j .. U S j + U S - 1 and the epilogue
+// writes them as contiguous pairs.  Its width is its slot count rounded up
+// to even (pairs never straddle two bundles).
+struct TcBundle {
+  std::vector<TcSlotX> slots;
+  int64_t start;  // earliest window start of its slots
+  int64_t end;    // latest window end
+  int width;
+};
+
+inline std::vector<TcBundle> tc_bundles(const TcGroupIn& g, int S) {
   std::vector<TcSlotX> xs;
   for (const TcSlotIn& s : g.slots) {
     for (int b = 0; b < S; ++b) {
@@ -138,39 +152,61 @@ inline std::vector<TcSlotX> tc_split_slots(const TcGroupIn& g, int S) {
     }
   }
   std::stable_sort(xs.begin(), xs.end(), [](const TcSlotX& a, const TcSlotX& b) {
-    return a.start != b.start ? a.start < b.start : a.s.delta < b.s.delta;
+    return a.s.ch != b.s.ch ? a.s.ch < b.s.ch : a.s.r < b.s.r;
   });
-  return xs;
+  std::vector<TcBundle> bs;
+  for (size_t i = 0; i < xs.size();) {
+    size_t j = i;
+    TcBundle b;
+    b.start = xs[i].start;
+    b.end = xs[i].s.delta;
+    while (j < xs.size() && xs[j].s.ch == xs[i].s.ch) {
+      b.start = std::min(b.start, xs[j].start);
+      b.end = std::max(b.end, xs[j].s.delta);
+      b.slots.push_back(xs[j]);
+      ++j;
+    }
+    b.width = (int)((b.slots.size() + 1) & ~(size_t)1);
+    bs.push_back(b);
+    i = j;
+  }
+  std::stable_sort(bs.begin(), bs.end(), [](const TcBundle& a, const TcBundle& b) {
+    return a.start != b.start ? a.start < b.start : a.end < b.end;
+  });
+  return bs;
 }
 
-// Merge-set window of slots [i, j) (sorted by start): its start in
+// Merge-set window of bundles [i, j) (sorted by start): its start in
 // [history | block] samples rounded down to even, and its K chunks.
-inline void tc_window(const std::vector<TcSlotX>& xs, size_t i, size_t j, int H, int64_t* a, int64_t* chunks) {
-  int64_t st = xs[i].start + H;
+inline void tc_window(const std::vector<TcBundle>& bs, size_t i, size_t j, int H, int64_t* a, int64_t* chunks) {
+  int64_t st = bs[i].start + H;
   if (st & 1) st -= 1;
-  int64_t end = xs[i].s.delta;
-  for (size_t q = i + 1; q < j; ++q) end = std::max(end, xs[q].s.delta);
+  int64_t end = bs[i].end;
+  for (size_t q = i + 1; q < j; ++q) end = std::max(end, bs[q].end);
   *a = st;
   *chunks = (end + H - st + 1 + kTcChunkTaps - 1) / kTcChunkTaps;
 }
 
-// Partition of the sorted slots into merge sets of at most kTcMsetSlots
+// Partition of the sorted bundles into merge sets of at most kTcMsetSlots
 // slots minimising the total K chunks: one MMA of M = 128, K = 16 costs the
 // same for any N up to 256, so the work of a tile is its merge sets' chunks
 // (dynamic programming over the split points).  Returns the cut points and
-// the chunks per tile row.
-inline int64_t tc_partition(const std::vector<TcSlotX>& xs, int H, std::vector<size_t>& cuts) {
-  const size_t n = xs.size();
+// the chunks per tile row; -1 when a bundle alone exceeds a merge set.
+inline int64_t tc_partition(const std::vector<TcBundle>& bs, int H, std::vector<size_t>& cuts) {
+  const size_t n = bs.size();
   std::vector<int64_t> best(n + 1, INT64_MAX);
   std::vector<size_t> from(n + 1, 0);
   best[0] = 0;
   for (size_t i = 0; i < n; ++i) {
     if (best[i] == INT64_MAX) continue;
-    int64_t st = xs[i].start + H;
+    int64_t st = bs[i].start + H;
     if (st & 1) st -= 1;
-    int64_t end = xs[i].s.delta;
-    for (size_t j = i + 1; j <= n && (int)(j - i) <= kTcMsetSlots; ++j) {
-      end = std::max(end, xs[j - 1].s.delta);
+    int64_t end = bs[i].end;
+    int width = 0;
+    for (size_t j = i + 1; j <= n; ++j) {
+      width += bs[j - 1].width;
+      if (width > kTcMsetSlots) break;
+      end = std::max(end, bs[j - 1].end);
       const int64_t c = best[i] + (end + H - st + 1 + kTcChunkTaps - 1) / kTcChunkTaps;
       if (c < best[j]) {
         best[j] = c;
@@ -179,6 +215,7 @@ inline int64_t tc_partition(const std::vector<TcSlotX>& xs, int H, std::vector<s
     }
   }
   cuts.clear();
+  if (best[n] == INT64_MAX) return -1;
   for (size_t j = n; j > 0; j = from[j]) cuts.push_back(j);
   cuts.push_back(0);
   std::reverse(cuts.begin(), cuts.end());
@@ -187,26 +224,34 @@ inline int64_t tc_partition(const std::vector<TcSlotX>& xs, int H, std::vector<s
 
 // Row split of a group: the power of two up to max_split (S even for odd D,
 // so that rows start 16 bytes apart) with the fewest K chunks over all its
-// tiles (chunks per tile row x rows / S); ties keep the smaller split.  The
-// split slots stay within four full merge sets.
+// tiles (chunks per tile row x rows / S); ties keep the smaller split.  A
+// channel's bundle (U S slots) fits one merge set, and the group's slots
+// stay within four full merge sets.
 inline int tc_choose_split(const TcGroupIn& g, int H) {
   int64_t J = 0;
-  for (const TcSlotIn& s : g.slots) J = std::max(J, s.J);
+  int Umax = 1;
+  for (const TcSlotIn& s : g.slots) {
+    J = std::max(J, s.J);
+    Umax = std::max(Umax, s.U);
+  }
   int bestS = 0;
   double bestc = 0;
   for (int S = 1; S <= std::max(1, g.max_split); S *= 2) {
     if ((g.D & 1) && (S & 1)) continue;
+    if ((int64_t)Umax * S > kTcMsetSlots) break;
     if (S > 2 && (int64_t)g.slots.size() * S > 4 * kTcMsetSlots) break;
-    const std::vector<TcSlotX> xs = tc_split_slots(g, S);
-    if (xs.empty()) continue;
+    const std::vector<TcBundle> bs = tc_bundles(g, S);
+    if (bs.empty()) continue;
     std::vector<size_t> cuts;
-    const double c = (double)tc_partition(xs, H, cuts) * (double)((J + (int64_t)S * kTcRows - 1) / ((int64_t)S * kTcRows));
+    const int64_t ch = tc_partition(bs, H, cuts);
+    if (ch < 0) continue;
+    const double c = (double)ch * (double)((J + (int64_t)S * kTcRows - 1) / ((int64_t)S * kTcRows));
     if (bestS == 0 || c < bestc) {
       bestS = S;
       bestc = c;
     }
   }
-  return bestS == 0 ? ((g.D & 1) ? 2 : 1) : bestS;
+  return bestS;
 }
 
 // Returns 0 on success, -1 when the apply exceeds a launch's record limits
@@ -217,9 +262,10 @@ inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_
   for (const TcGroupIn& g : gin) {
     if (g.slots.empty()) continue;
     const int S = tc_choose_split(g, H);
+    if (S == 0) return -1;
     const int64_t Dp = (int64_t)S * g.D;
-    const std::vector<TcSlotX> xs = tc_split_slots(g, S);
-    if (xs.empty()) continue;
+    const std::vector<TcBundle> bs = tc_bundles(g, S);
+    if (bs.empty()) continue;
     if ((int)p.groups.size() >= kTcMaxGroups) return -1;
     const int gi = (int)p.groups.size();
     TcPlanGroup pg;
@@ -227,17 +273,19 @@ inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_
     pg.S = S;
     pg.Wx = 0;
     std::vector<size_t> cuts;
-    tc_partition(xs, H, cuts);
+    if (tc_partition(bs, H, cuts) < 0) return -1;
     for (size_t ci = 0; ci + 1 < cuts.size(); ++ci) {
       const size_t i = cuts[ci], j = cuts[ci + 1];
       int64_t a, nchunks;
-      tc_window(xs, i, j, H, &a, &nchunks);
-      const int nreal = (int)(j - i);
+      tc_window(bs, i, j, H, &a, &nchunks);
+      int width = 0;
+      for (size_t q = i; q < j; ++q) width += bs[q].width;
       // record field ranges (16-bit taps, strides and offsets)
       if (nchunks * kTcChunkTaps > 65535) return -1;
       for (size_t q = i; q < j; ++q)
-        if (xs[q].s.T > 65535 || xs[q].s.U > 65535 || xs[q].s.phi > 65535 || xs[q].s.J > INT32_MAX) return -1;
-      const int NS = (int)tc_round_up(nreal, 8);
+        for (const TcSlotX& x : bs[q].slots)
+          if (x.s.T > 65535 || x.s.U > 65535 || x.s.phi > 65535 || x.s.J > INT32_MAX) return -1;
+      const int NS = (int)tc_round_up(width, 8);
       if ((int)p.ms.size() >= kTcMaxMsets || (int)p.slots.size() + NS > kTcMaxSlots) return -1;
       TcMset m{};
       m.a = (int32_t)a;
@@ -248,20 +296,29 @@ inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_
       m.R = (int16_t)(4 * NS <= 128 ? 2 : 1);
       int64_t Jmax = 0;
       for (size_t q = i; q < j; ++q) {
-        const TcSlotX& x = xs[q];
-        TcSlot s{};
-        s.w0 = (int32_t)x.start;
-        s.J = (int32_t)x.s.J;
-        s.ch = (uint16_t)x.s.ch;
-        s.T = (uint16_t)x.s.T;
-        s.U = (uint16_t)x.s.U;
-        s.o = (uint16_t)(x.start + H - a);
-        s.phi = (uint16_t)x.s.phi;
-        p.slots.push_back(s);
-        p.slot_r.push_back(x.s.r);
-        Jmax = std::max(Jmax, x.s.J);
+        const TcBundle& b = bs[q];
+        for (size_t k = 0; k < b.slots.size(); ++k) {
+          const TcSlotX& x = b.slots[k];
+          TcSlot s{};
+          s.w0 = (int32_t)x.start;
+          s.J = (int32_t)x.s.J;
+          s.ch = (uint16_t)x.s.ch;
+          s.T = (uint16_t)x.s.T;
+          s.U = (uint16_t)x.s.U;
+          s.o = (uint16_t)(x.start + H - a);
+          s.phi = (uint16_t)x.s.phi;
+          // even slot followed by the channel's next output: one 16-byte store
+          s.flags = (k % 2 == 0 && k + 1 < b.slots.size() && b.slots[k + 1].s.r == x.s.r + 1) ? 1 : 0;
+          p.slots.push_back(s);
+          p.slot_r.push_back(x.s.r);
+          Jmax = std::max(Jmax, x.s.J);
+        }
+        if (b.slots.size() & 1) {
+          p.slots.push_back(TcSlot{});
+          p.slot_r.push_back(0);
+        }
       }
-      for (int q = nreal; q < NS; ++q) {
+      for (int q = width; q < NS; ++q) {
         p.slots.push_back(TcSlot{});
         p.slot_r.push_back(0);
       }

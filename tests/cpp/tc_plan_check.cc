@@ -165,6 +165,12 @@ int main(int argc, char** argv) {
         Jmax = std::max<int64_t>(Jmax, sl.J);
         CHECK(sl.o + sl.T <= Kw, "slot window in merged window: o %d T %d Kw %lld", sl.o, sl.T, (long long)Kw);
         CHECK(m.a + sl.o == (int64_t)sl.w0 + H, "slot offset");
+        if (sl.flags & 1) {  // pair store: the next slot is the same channel's next output
+          const TcSlot& nx = p.slots[m.slot0 + s + 1];
+          CHECK(s % 2 == 0 && s + 1 < m.NS && nx.J > 0 && nx.ch == sl.ch && nx.U == sl.U &&
+                    p.slot_r[m.slot0 + s + 1] == p.slot_r[m.slot0 + s] + 1 && nx.J <= sl.J && nx.J + 1 >= sl.J,
+                "pair flag");
+        }
         // the last valid row reads only [history | block] and lies inside the map
         const int64_t jl = sl.J - 1;
         const int64_t first = jl * D + sl.w0 + H, last = first + sl.T - 1;
