@@ -14,13 +14,19 @@ Reported (one JSON line, rank 0):
   e2e        The same metric through the C ABI's host-buffer call
              (fdsp_channelizer_apply_host): pinned host input -> H2D -> kernels
              -> D2H of every output sample, per step.
-  roofline   Dominant kernel (the fused shift+resample kernel) against the
-             measured HBM copy bandwidth: algorithmic bytes per launch
-             (8 B per input sample + 8 B per output sample) / launch time.
+  roofline   Dominant kernel (tc_filter_kernel, the tensor-core filter bank;
+             tc_prep_kernel splits the input beside it) against the measured
+             HBM copy bandwidth: algorithmic bytes of a step (8 B per input
+             sample + 8 B per output sample) / the summed duration of the
+             step's tc_filter_kernel launches, timed live with CUDA events on
+             the launch stream; traffic from the committed ncu summary
+             (profiles/*_dram.txt, written by libfalcon_dsp_gb300.ncu_summary
+             from ncu's CSV output).
   cpu_baseline  The reference CPU channelizer path (oracle/_ref when built from
              the reference sources, else the oracle's C restatement) on a
-             bounded sample of the same workload, channels spread over host
-             threads.
+             bounded sample of the same workload (the same sample length as
+             the reference arm), channels spread over all host threads, and
+             on one thread.
 Multi-GPU: replicas only -- every rank runs the same workload on its own GPU,
 with no collective on the data path; value sums ranks.
 
@@ -66,6 +72,7 @@ def parse():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-other-configs", action="store_true")
+    ap.add_argument("--no-kernel-timing", action="store_true", help="skip the per-kernel CUDA-event pass")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--serve-streams", type=int, default=16, help="concurrent streams the server admits")
     return ap.parse_args()
@@ -126,15 +133,41 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def ncu_traffic(name: str, n_in: int):
-    """DRAM bytes per launch from the committed ncu summary of this kernel and
-    workload (profiles/<name>.md, line 'dram_bytes_per_input_sample: X'),
-    scaled to n_in input samples; None when no capture was summarised."""
-    p = os.path.join(ROOT, "profiles", f"{name}.md")
+def ncu_traffic(summary: str, kernel: str, n_in: int):
+    """DRAM bytes of one step's launches of `kernel`, from the committed ncu
+    summary (profiles/<summary>.txt, written by libfalcon_dsp_gb300.ncu_summary
+    from ncu's CSV) scaled to n_in input samples; with the whole step's bytes
+    per input sample.  None when no capture was summarised."""
+    from libfalcon_dsp_gb300 import ncu_summary
+    p = os.path.join(ROOT, "profiles", f"{summary}.txt")
     if not os.path.exists(p):
         return None
-    m = re.search(r"dram_bytes_per_input_sample:\s*([0-9.eE+-]+)", open(p).read())
-    return float(m.group(1)) * n_in if m else None
+    d = ncu_summary.read(p)
+    k = d.get(f"{kernel}.dram_bytes_per_input_sample")
+    if k is None:
+        return None
+    return {"bytes_per_step": round(k * n_in), "bytes_per_input_sample": round(k, 2),
+            "step_bytes_per_input_sample": round(d.get("step.dram_bytes_per_input_sample", 0.0), 2),
+            "captured_n_in": int(d.get("n_in", 0)), "source": f"profiles/{summary}.txt"}
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith("model name"):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
 
 
 def cpu_threads() -> int:
@@ -169,6 +202,18 @@ def cpu_channelizer_rate(fs, chans, x, threads, use_reference: bool) -> tuple[fl
     return tot / dt / 1e6, kind, threads
 
 
+def cpu_baseline(fs, chans, x, use_reference: bool, single_thread: bool = True) -> dict:
+    """The CPU leg on sample x: channel-parallel over every host thread, and
+    (single_thread) the same sample on one thread."""
+    rate, kind, used = cpu_channelizer_rate(fs, chans, x, cpu_threads(), use_reference)
+    out = {"value": round(rate, 3), "unit": "Msamples/s", "cores": used, "kind": kind, "cpu_model": cpu_model(),
+           "sample": f"{x.size} input samples of the workload x {len(chans)} channels, channels over {used} threads"}
+    if single_thread:
+        r1, _, _ = cpu_channelizer_rate(fs, chans, x, 1, use_reference)
+        out["single_thread"] = {"value": round(r1, 3), "unit": "Msamples/s", "cores": 1}
+    return out
+
+
 def _time_device(fn, reps: int = 5, warm: int = 3):
     """Median ms of fn() over reps runs, CUDA events on the current stream."""
     import torch
@@ -186,12 +231,29 @@ def _time_device(fn, reps: int = 5, warm: int = 3):
     return float(np.median(ts)), out
 
 
-def other_configs(dev) -> dict:
+def fp64_fm_chain(x, h, down: int):
+    """FP64 arm of the long-FIR chain, for comparison only (library FFT
+    convolution in complex128 on the GPU, then the polar discriminator in
+    FP64): y[m] = sum_k h[k] x[m D - k] from a zero history, as the
+    resampler's first apply computes it."""
+    import torch
+    n, t = x.numel(), h.size
+    nf = 1 << (n + t - 1 - 1).bit_length()
+    X = torch.fft.fft(x.to(torch.complex128), nf)
+    H = torch.fft.fft(torch.from_numpy(h.astype(np.complex128)).to(x.device), nf)
+    y = torch.fft.ifft(X * H)[:n:down]
+    del X, H
+    return y, torch.angle(y[1:] * torch.conj(y[:-1]))
+
+
+def other_configs(dev, lib) -> dict:
     import torch
 
     import libfalcon_dsp_gb300 as F
     from libfalcon_dsp_gb300.workloads import audio_snr_db, channelizer_8ch, fm_chain, resampler_1ch
     res = {}
+    pk = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     # single-channel resampler 48 kHz -> 44.1 kHz, 2^20 samples, 3528 taps
     x, up, down, h = resampler_1ch(1 << 20, 2024, device=dev)
     rs = F.PolyphaseResamplerCuda(up, down, h)
@@ -203,43 +265,77 @@ def other_configs(dev) -> dict:
     ms, n_out = _time_device(c1)
     res["resampler_147_160"] = {"n_in": x.numel(), "n_out": n_out, "ms": round(ms, 4),
                                 "value": round(n_out / ms / 1e3, 1), "unit": "Msamples/s"}
-    # 8-channel channelizer, 2^24 samples streamed in 2^16-sample blocks
+    # 8-channel channelizer over 16 QPSK carriers, 2^24 samples streamed in
+    # 2^16-sample blocks through the C ABI's device-buffer call
     x, fs, chans = channelizer_8ch(1 << 24, 2025, device=dev)
     ch = F.MultiRateChannelizerCuda(fs, chans)
     blk = 1 << 16
-    outs = [torch.empty(c + 2, dtype=torch.complex64, device=dev) for c in ch.out_count(blk)]
+    nch = len(chans)
+    caps = [c + 2 for c in ch.out_count(blk)]
+    outs = [torch.empty(c, dtype=torch.complex64, device=dev) for c in caps]
+    optr = (C.c_void_p * nch)(*[o.data_ptr() for o in outs])
+    cap_arr = (C.c_uint64 * nch)(*caps)
+    n_out_arr = (C.c_uint64 * nch)()
     s = torch.cuda.Stream(device=dev)
+    sh = C.c_void_p(s.cuda_stream)
     ch.set_graph(True)
+    xptrs = [C.c_void_p(x[b * blk:].data_ptr()) for b in range(x.numel() // blk)]
 
     def c2():
         ch.reset_state()
         tot = 0
-        with torch.cuda.stream(s):
-            for b in range(x.numel() // blk):
-                tot += sum(y.numel() for y in ch.apply(x[b * blk:(b + 1) * blk], out=outs))
+        s.wait_stream(torch.cuda.current_stream())
+        for xp in xptrs:
+            st = lib.fdsp_channelizer_apply(ch._h, xp, blk, optr, cap_arr, n_out_arr, sh)
+            if st != 0:
+                raise F.FdspError("fdsp_channelizer_apply", st, lib.fdsp_last_cuda_error())
+            tot += sum(n_out_arr)
         torch.cuda.current_stream().wait_stream(s)
         return tot
     ms, n_out = _time_device(c2, reps=3, warm=1)
-    res["channelizer_8ch_blocks_2p16"] = {"n_in": x.numel(), "blocks": x.numel() // blk, "n_out": n_out,
-                                          "ms": round(ms, 3), "value": round(n_out / ms / 1e3, 1),
-                                          "unit": "Msamples/s", "cuda_graph": True}
-    # FIR 4095 taps / decimate 10 / polar discriminator, 2^26 samples
+    res["channelizer_8ch_qpsk_blocks_2p16"] = {
+        "n_in": x.numel(), "blocks": x.numel() // blk, "n_out": n_out, "ms": round(ms, 3),
+        "value": round(n_out / ms / 1e3, 1), "unit": "Msamples/s", "cuda_graph": True,
+        "call": "fdsp_channelizer_apply (device buffers), one call per 2^16-sample block"}
+    del x, outs
+    # FIR 4095 taps / decimate 10 / polar discriminator, 2^26 samples: the
+    # tensor-core forms, plain FP32 and an FP64 comparison arm
     x, fs, h, tones = fm_chain(1 << 26, 2027, device=dev)
     rs = F.PolyphaseResamplerCuda(1, 10, h)
     pd = F.PolarDiscriminatorCuda()
     y = torch.empty(rs.out_count(x.numel()) + 2, dtype=torch.complex64, device=dev)
     a = torch.empty(y.numel() + 2, dtype=torch.float32, device=dev)
+    fm = {"n_in": x.numel(), "taps": int(h.size), "down": 10}
+    for mode in ("fp16x3", "bf16x3", "fp32"):
+        rs.set_precision(mode)
 
-    def c5():
-        rs.reset_state()
-        pd.reset_state()
-        yy = rs.apply(x, out=y)
-        return pd.apply(yy, out=a).numel()
-    ms, n_aud = _time_device(c5, reps=3, warm=1)
-    snr = audio_snr_db(a[:n_aud].cpu().numpy(), fs / 10, tones)
-    res["fir4095_dec10_fm"] = {"n_in": x.numel(), "n_audio": n_aud, "ms": round(ms, 3),
-                               "value": round(x.numel() / ms / 1e3, 1), "unit": "input Msamples/s",
-                               "audio_snr_db": round(snr, 2), "fir_gflops": round(4 * 4095 * (n_aud + 1) / ms / 1e6, 1)}
+        def c5():
+            rs.reset_state()
+            pd.reset_state()
+            yy = rs.apply(x, out=y)
+            return pd.apply(yy, out=a).numel()
+        ms, n_aud = _time_device(c5, reps=3, warm=1)
+        snr = audio_snr_db(a[:n_aud].cpu().numpy(), fs / 10, tones)
+        useful = 8.0 * h.size * (n_aud + 1)  # complex tap x complex sample: 8 flops
+        arm = {"ms": round(ms, 3), "value": round(x.numel() / ms / 1e3, 1), "unit": "input Msamples/s",
+               "audio_snr_db": round(snr, 2), "fir_tflops": round(useful / ms / 1e9, 2)}
+        if mode != "fp32":
+            arm["tensor_core"] = bool(rs.tc_groups())
+            if pk.get("bf16_tflops_sustained"):
+                arm["fir_tflops_frac_of_bf16_sustained"] = round(useful / ms / 1e9 / pk["bf16_tflops_sustained"], 4)
+        fm[mode] = arm
+    rs.set_precision("fp32")
+
+    def c64():
+        return fp64_fm_chain(x, h, 10)[1].numel()
+    ms, _ = _time_device(c64, reps=1, warm=1)
+    _, a64 = fp64_fm_chain(x, h, 10)
+    fm["fp64"] = {"ms": round(ms, 3), "value": round(x.numel() / ms / 1e3, 1), "unit": "input Msamples/s",
+                  "audio_snr_db": round(audio_snr_db(a64.cpu().numpy(), fs / 10, tones), 2),
+                  "how": "torch complex128 FFT convolution + FP64 discriminator on the GPU (comparison arm)"}
+    del a64
+    res["fir4095_dec10_fm"] = fm
+    del x
     # standalone complex FIR, 64 complex taps at full rate, 2^26 samples: the
     # FP32 kernel and the tensor-core Toeplitz form (fp16 hi+lo)
     g = torch.Generator(device="cpu").manual_seed(2030)
@@ -286,7 +382,7 @@ def run_reference(args) -> None:
     from libfalcon_dsp_gb300.workloads import channelizer_256_cpu_sample
     from oracle import oracle as O
     O.build()
-    n = args.cpu_sample // 4
+    n = args.cpu_sample
     x, fs, chans = channelizer_256_cpu_sample(n, args.n, SEED)
     use_ref = O.have_reference()
     threads = cpu_threads()
@@ -299,13 +395,15 @@ def run_reference(args) -> None:
         rates.append(r)
     wall = time.perf_counter() - t0
     value = float(np.median(rates))
+    r1, _, _ = cpu_channelizer_rate(fs, chans, x, 1, use_ref)
     line = {
         "impl": "reference", "metric": "channelizer output Msamples/s", "value": value, "unit": "Msamples/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample": f"{n} input samples per step x 256 channels", "seed": SEED},
         "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": used, "kind": kind,
-                         "sample": f"{n} input samples x 256 channels per step"},
+                         "cpu_model": cpu_model(), "sample": f"{n} input samples x 256 channels per step",
+                         "single_thread": {"value": round(r1, 3), "unit": "Msamples/s", "cores": 1}},
         "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -405,17 +503,33 @@ def run_ours(args) -> None:
     ms_per_step = ms / args.steps
     value = outputs_all / (ms / 1e3) / 1e6
 
-    # roofline of the fused kernel (the hist-update launch per step moves < 1 KB)
-    bytes_per_launch = algorithmic_bytes(x.numel(), outputs // args.steps)
-    achieved_gbs = bytes_per_launch / (ms_per_step / 1e3) / 1e9
-    pk = peaks()
-    kname = "poly_tc_kernel" if any(t["tensor_core"] for t in tune) else "poly_fp32_kernel"
-    traffic = ncu_traffic(f"{kname}_channelizer_256", x.numel())
-    roof = {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": round(achieved_gbs / pk["hbm_gbs"], 4), "traffic": traffic,
-            "kernel": kname, "peak_source": pk["source"],
-            "bytes_per_launch": bytes_per_launch,
-            "note": "one step = one launch per decimation group (12) + one history update; achieved uses the step time"}
+    # roofline of the dominant kernel: its launches of a step timed live with
+    # CUDA events on the launch stream (direct launches while timing)
+    bytes_per_step = algorithmic_bytes(x.numel(), outputs // args.steps)
+    kname = "tc_filter_kernel" if args.precision != "fp32" else "poly_fp32_kernel"
+    roof = None
+    if not args.no_kernel_timing:
+        ch.set_profile(True)
+        for _ in range(args.steps):
+            step()
+        kms, kl = ch.read_profile()
+        ch.set_profile(False)
+        if world > 1:
+            kms, _ = replica_aggregate(kms, 0, world, dev)
+        kms_step = kms / args.steps
+        achieved_gbs = bytes_per_step / (kms_step / 1e3) / 1e9
+        pk = peaks()
+        traffic = ncu_traffic(f"{kname}_channelizer_256_dram", kname, x.numel())
+        roof = {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved_gbs / pk["hbm_gbs"], 4),
+                "traffic": traffic["bytes_per_step"] if traffic else None, "traffic_detail": traffic,
+                "kernel": kname, "peak_source": pk["source"] + " (burst copy)",
+                "kernel_ms_per_step": round(kms_step, 4), "kernel_launches_per_step": kl // max(args.steps, 1),
+                "kernel_share_of_step": round(kms_step / ms_per_step, 3),
+                "algorithmic_bytes_per_step": bytes_per_step,
+                "note": "achieved = algorithmic bytes of a step (input read once + every output written once) / "
+                        "summed duration of the step's launches of the kernel; traffic = DRAM bytes of those "
+                        "launches (ncu, scaled by input samples)"}
 
     # end to end through the host-buffer C ABI call (pinned host memory)
     e2e = None
@@ -453,7 +567,7 @@ def run_ours(args) -> None:
     # FIR / decimate-by-10 / FM discriminator chain
     others = None
     if not args.no_other_configs:
-        others = other_configs(dev)
+        others = other_configs(dev, lib)
 
     # streaming serving loop: Poisson job arrivals at 2000/s, 1-64 channels,
     # blocks of 4096-1M samples, host buffers in and out, FP32 form
@@ -475,10 +589,7 @@ def run_ours(args) -> None:
         from oracle import oracle as O
         O.build(with_reference=None)
         n_s = min(args.cpu_sample, x.numel())
-        xs = x[:n_s].cpu().numpy()
-        rate, kind, used = cpu_channelizer_rate(fs, chans, xs, cpu_threads(), O.have_reference())
-        cpu = {"value": round(rate, 3), "unit": "Msamples/s", "cores": used, "kind": kind,
-               "sample": f"first {n_s} input samples of the workload x 256 channels, channels over {used} threads"}
+        cpu = cpu_baseline(fs, chans, x[:n_s].cpu().numpy(), O.have_reference())
 
     if rank == 0:
         line = {

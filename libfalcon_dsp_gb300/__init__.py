@@ -228,6 +228,18 @@ class MultiRateChannelizerCuda(_Handle):
         _capi.call("fdsp_channelizer_kernel_launches", self._h, C.byref(v))
         return v.value
 
+    def set_profile(self, enable: bool = True) -> None:
+        """Time every filter-bank launch of later applies with CUDA events on
+        the apply's stream (applies launch directly, no graph); enabling
+        restarts the record."""
+        _capi.call("fdsp_channelizer_profile", self._h, 1 if enable else 0)
+
+    def read_profile(self) -> tuple[float, int]:
+        """(summed milliseconds, launches) of the timed filter-bank launches."""
+        ms, n = C.c_double(), C.c_uint32()
+        _capi.call("fdsp_channelizer_profile_read", self._h, C.byref(ms), C.byref(n))
+        return ms.value, n.value
+
     def autotune(self, n_in: int, stream: int | None = None) -> list[dict]:
         """Time each decimation group on an n_in-sample block and keep the
         fastest FP32 tile height per group; resets the streaming state.

@@ -236,7 +236,7 @@ inline int tc_choose_split(const TcGroupIn& g, int H) {
   }
   int bestS = 0;
   double bestc = 0;
-  for (int S = 1; S <= std::max(1, g.max_split); S *= 2) {
+  for (int S = 1; S <= std::max((g.D & 1) ? 2 : 1, g.max_split); S *= 2) {
     if ((g.D & 1) && (S & 1)) continue;
     if ((int64_t)Umax * S > kTcMsetSlots) break;
     if (S > 2 && (int64_t)g.slots.size() * S > 4 * kTcMsetSlots) break;

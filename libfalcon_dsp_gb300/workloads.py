@@ -10,10 +10,12 @@ shapes, rates and value distributions of the benchmark configurations.
   channel's NCO brings one tone to DC.
 * ``resampler_1ch``    2^20 samples at 48 kHz (3 tones + noise), 147/160,
   Kaiser sinc beta 8.6 with 3528 taps (24 per phase).
-* ``channelizer_8ch``  2^24 samples at 10 MSps (tones stand in for the QPSK
-  carriers of the spec at the same centre-frequency spread), 8 channels with
-  ratios 1/40, 3/125, 1/80, 2/625, 1/50, 1/20, 3/200, 1/100, 16-48 taps per
-  phase, streamed in 2^16-sample blocks.
+* ``channelizer_8ch``  2^24 samples at 10 MSps: 16 QPSK carriers (random
+  centre frequencies in +-4.5 MHz, symbol rates 25-250 kBd drawn as whole
+  samples per symbol, root-raised-cosine pulses with roll-off 0.35, unit power
+  each) plus AWGN 20 dB below each carrier's power; 8 channels with ratios
+  1/40, 3/125, 1/80, 2/625, 1/50, 1/20, 3/200, 1/100, each shifting one
+  carrier to DC, 16-48 taps per phase, streamed in 2^16-sample blocks.
 
 Tones sit on the frequency grid of the signal length so a whole signal is one
 inverse FFT of a sparse spectrum (fast at 2^26 samples).
@@ -118,9 +120,57 @@ def resampler_1ch(n: int = 1 << 20, seed: int = 2024, device=None):
 C2_RATIOS = [(1, 40), (3, 125), (1, 80), (2, 625), (1, 50), (1, 20), (3, 200), (1, 100)]
 
 
+def rrc_spectrum(f: np.ndarray, symbol_rate: float, alpha: float = 0.35) -> np.ndarray:
+    """Root-raised-cosine frequency response (1 in the passband) at
+    frequencies f (Hz) for the given symbol rate and roll-off."""
+    af = np.abs(f) / symbol_rate
+    lo, hi = (1 - alpha) / 2, (1 + alpha) / 2
+    h = np.zeros(f.shape)
+    h[af <= lo] = 1.0
+    mid = (af > lo) & (af < hi)
+    h[mid] = np.sqrt(0.5 * (1 + np.cos(np.pi / alpha * (af[mid] - lo))))
+    return h
+
+
+def qpsk_carriers(n: int, fs: float, carriers: int, seed: int, max_freq: float, min_baud: float = 25e3,
+                  max_baud: float = 250e3, alpha: float = 0.35, snr_db: float = 20.0):
+    """Sum of `carriers` QPSK carriers with root-raised-cosine pulses plus
+    AWGN, synthesised as one circular band-limited signal of n samples.
+
+    A carrier carries nsym symbols over the n samples (symbol rate fs nsym / n,
+    drawn in [min_baud, max_baud]); a band-limited pulse train with period n
+    has at bin k the nsym-point DFT of the symbols at k mod nsym times the
+    pulse's response at k fs / n, so each carrier is filled in over its own
+    band only, scaled to unit power (Parseval) and moved to a centre frequency
+    on the fs/n grid.  Noise power is 10^(-snr_db/10) relative to one carrier.
+    Returns (x complex64, centre frequencies in Hz)."""
+    from scipy import fft as sfft
+    rng = np.random.default_rng(seed)
+    spec = np.zeros(n, np.complex128)
+    freqs = np.empty(carriers)
+    const = np.exp(1j * np.pi * (np.arange(4) / 2 + 0.25))
+    for c in range(carriers):
+        nsym = int(rng.integers(int(np.ceil(min_baud * n / fs)), int(max_baud * n / fs) + 1))
+        A = sfft.fft(const[rng.integers(0, 4, nsym)])
+        kb = int((1 + alpha) / 2 * nsym)
+        k = np.arange(-kb, kb + 1)
+        S = A[k % nsym] * rrc_spectrum(k * (fs / n), fs * nsym / n, alpha)
+        S *= np.sqrt(n * n / max(np.sum(np.abs(S) ** 2), 1e-300))  # unit mean power
+        kc = int(rng.integers(-int(max_freq / fs * n) + kb, int(max_freq / fs * n) - kb + 1))
+        freqs[c] = kc * fs / n
+        np.add.at(spec, (k + kc) % n, S)
+    x = sfft.ifft(spec, workers=-1)
+    sigma = np.sqrt(10 ** (-snr_db / 10) / 2)
+    x += sigma * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    return (0.25 * x).astype(np.complex64), freqs
+
+
 def channelizer_8ch(n: int = 1 << 24, seed: int = 2025, device=None):
     fs = 10e6
-    x, freqs = tone_signal(n, fs, 16, seed, max_freq=4.5e6, device=device)
+    x, freqs = qpsk_carriers(n, fs, 16, seed, 4.5e6)
+    if device is not None:
+        import torch
+        x = torch.from_numpy(x).to(device)
     rng = np.random.default_rng(seed + 1)
     chans = []
     for c, (u, d) in enumerate(C2_RATIOS):

@@ -37,3 +37,40 @@ def test_fm_chain_matches_oracle_and_recovers_audio():
     snr = audio_snr_db(np.concatenate(audio), fs / 10, tones)
     print(f"recovered audio SNR {snr:.1f} dB")
     assert snr >= 20.0
+
+
+@pytest.mark.parametrize("mode", ["fp16x3", "bf16x3"])
+def test_fm_chain_tensor_core_vs_fp64(mode):
+    """The same chain with the 4095-tap resampler on the tensor cores (split
+    precision, FP32 accumulation, K chunked over 256 chunks of 16 taps):
+    streamed in 2^16-sample blocks, every block's resampler output >= 60 dB
+    SNR against the FP64 oracle, counts exact, the tensor-core form really
+    ran, and the recovered audio keeps its SNR within 0.5 dB of the FP64
+    chain's."""
+    torch = pytest.importorskip("torch")
+    from tests.golden_io import snr_db
+    n, blk = 1 << 18, 1 << 16
+    x, fs, h, tones = fm_chain(n, seed=12)
+    rs = F.PolyphaseResamplerCuda(1, 10, h)
+    rs.set_precision(mode)
+    pd = F.PolarDiscriminatorCuda()
+    o64 = O.Resampler(1, 10, h)
+    xd = torch.from_numpy(x).cuda()
+    audio, y64s, worst = [], [], 1e9
+    for b in range(n // blk):
+        y = rs.apply(xd[b * blk:(b + 1) * blk])
+        a = pd.apply(y)
+        assert rs.tc_groups() == 1
+        y64 = o64.apply64(x[b * blk:(b + 1) * blk])
+        assert y.numel() == y64.size
+        worst = min(worst, snr_db(y.cpu().numpy(), y64))
+        audio.append(a.cpu().numpy())
+        y64s.append(y64)
+    rs.status()  # raises on a tensor-core timeout
+    yy = np.concatenate(y64s)
+    a64 = np.angle(yy[1:] * np.conj(yy[:-1]))
+    snr_tc = audio_snr_db(np.concatenate(audio), fs / 10, tones)
+    snr_64 = audio_snr_db(a64, fs / 10, tones)
+    print(f"{mode}: worst block SNR vs FP64 {worst:.1f} dB; audio SNR {snr_tc:.2f} dB (FP64 chain {snr_64:.2f} dB)")
+    assert worst >= 60.0, worst
+    assert abs(snr_tc - snr_64) <= 0.5

@@ -7,7 +7,7 @@ combine an oracle check on a prefix with size-independent properties:
   * scaling the input by 2 scales every output by exactly 2 (bit-exact);
   * the tensor-core forms stay >= 60 dB SNR from the plain FP32 form;
   * on a prefix, every channel matches the oracle (FP32 <= 1e-5 relative RMS,
-    tensor cores >= 60 dB SNR against the FP64 oracle).
+    tensor cores above a per-form SNR floor against the FP64 oracle).
 """
 import numpy as np
 import pytest
@@ -114,14 +114,24 @@ def test_full_size_tensor_core_vs_fp32(full, mode):
             assert float(10 * torch.log10(torch.linalg.vector_norm(b) ** 2 / err)) >= 100.0
 
 
-def test_full_size_prefix_matches_oracle(full):
+# Per-form SNR floors against the FP64 oracle (dB): the lowest channel
+# measured on the GB300 minus a 3 dB margin.
+TC_FLOOR_DB = {"fp16x3": 60.0, "bf16x3": 60.0}
+
+
+@pytest.mark.parametrize("mode", ["fp16x3", "bf16x3"])
+def test_full_size_prefix_matches_oracle(full, mode):
+    """Every one of the 256 channels of the full-size tensor-core run, on the
+    outputs of the first 2^16 input samples, against the FP64 oracle."""
     torch, x, fs, chans = full
-    ys = _run(F, torch, x, fs, chans, "fp16x3")
+    ys = _run(F, torch, x, fs, chans, mode)
     n = 1 << 16
     xp = x[:n].cpu().numpy()
-    sub = list(range(0, 256, 16))
-    o64 = O.Channelizer(fs, [chans[i] for i in sub], precision="f64").apply(xp)
-    for i, b in zip(sub, o64):
+    o64 = O.Channelizer(fs, chans, precision="f64").apply(xp)
+    snrs = []
+    for y, b in zip(ys, o64):
         # outputs of the prefix depend only on the prefix (no lookahead)
-        a = ys[i][: b.size].cpu().numpy()
-        assert snr_db(a, b) >= 60.0
+        a = y[: b.size].cpu().numpy()
+        snrs.append(snr_db(a, b))
+    print(f"{mode}: SNR vs FP64 over 256 channels: min {min(snrs):.1f} median {np.median(snrs):.1f} dB")
+    assert min(snrs) >= TC_FLOOR_DB[mode], (mode, min(snrs))
