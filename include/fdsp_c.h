@@ -198,6 +198,11 @@ int fdsp_channelizer_status(fdsp_channelizer *h, fdsp_stream_t stream);
  * withhold_copies != 0 makes later launches issue no operand copies, so every
  * wait runs out: a test hook for the timeout path, never for production. */
 int fdsp_channelizer_set_tc_wait(fdsp_channelizer *h, uint32_t max_polls, int withhold_copies);
+/* Test hook of the tensor-core kernel's exact rotation pass: on != 0 makes
+ * every output of later applies take it (as slots whose row stride spans
+ * more than the NCO rollover do), instead of only the windows that straddle
+ * the rollover.  Results stay within the tensor-core bound; slower. */
+int fdsp_channelizer_set_tc_exact_all(fdsp_channelizer *h, int on);
 /* Kernel timing (diagnostics, no counterpart in the reference): while
  * enabled, applies launch directly (no graph) and each filter-bank launch
  * (tensor-core or FP32 kernel) is bracketed by CUDA events on the apply's

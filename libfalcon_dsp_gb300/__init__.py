@@ -223,6 +223,11 @@ class MultiRateChannelizerCuda(_Handle):
         hook that makes every wait run out."""
         _capi.call("fdsp_channelizer_set_tc_wait", self._h, int(max_polls), 1 if withhold_copies else 0)
 
+    def set_tc_exact_all(self, on: bool = True) -> None:
+        """Test hook: every output takes the tensor-core kernel's exact
+        rotation pass (as slots whose row stride spans the NCO rollover do)."""
+        _capi.call("fdsp_channelizer_set_tc_exact_all", self._h, 1 if on else 0)
+
     def kernel_launches(self) -> int:
         v = C.c_uint32()
         _capi.call("fdsp_channelizer_kernel_launches", self._h, C.byref(v))

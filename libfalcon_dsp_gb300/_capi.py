@@ -89,6 +89,7 @@ SIGNATURES = {
     "fdsp_channelizer_tc_groups": [_vp, _pu32],
     "fdsp_channelizer_status": [_vp, _vp],
     "fdsp_channelizer_set_tc_wait": [_vp, _u32, C.c_int],
+    "fdsp_channelizer_set_tc_exact_all": [_vp, C.c_int],
     "fdsp_channelizer_profile": [_vp, C.c_int],
     "fdsp_channelizer_profile_read": [_vp, _pdbl, _pu32],
     "fdsp_resampler_set_precision": [_vp, C.c_int],

@@ -220,6 +220,12 @@ int fdsp_channelizer_status(fdsp_channelizer* h, fdsp_stream_t stream) {
   return engine_status(h->eng, (cudaStream_t)stream);
 }
 
+int fdsp_channelizer_set_tc_exact_all(fdsp_channelizer* h, int on) {
+  if (!h) return FDSP_ERR_NOT_INITIALIZED;
+  h->eng.set_tc_exact_all(on != 0 ? 1 : 0);
+  return FDSP_OK;
+}
+
 int fdsp_channelizer_set_tc_wait(fdsp_channelizer* h, uint32_t max_polls, int withhold_copies) {
   if (!h) return FDSP_ERR_NOT_INITIALIZED;
   if (max_polls == 0) return FDSP_ERR_INVALID_ARG;

@@ -15,18 +15,24 @@
 //      hi taps in the first half of the columns and lo taps in the second,
 //      prebuilt per apply in the same swizzled image and copied per chunk;
 //   Y  FP32 in tensor memory; the epilogue adds the hi and lo halves,
-//      rotates by the NCO phase of each window start (exact integer phase,
-//      split-sum fix for windows across the NCO rollover) and stores.
+//      rotates by the NCO phase of each window start (exact integer phase)
+//      and stores.  Windows across the NCO rollover are stored unrotated and
+//      rotated exactly (split sum) by tc_fix_kernel, launched after the
+//      filter bank: keeping that rare path out of the filter-bank kernel
+//      roughly halved its MMA issue time.
 //
-// Per CTA (one per SM, 320 threads):
-//   warp 0      producer: per item (R tiles of one merge set) and K chunk,
+// Per CTA (one per SM, 576 threads):
+//   warp 0      producer: walks the CTA's item sequence (shared-memory
+//               cursor) and announces each item in a ring with its first
+//               stage; per item (R tiles of one merge set) and K chunk,
 //               waits for a free stage, then R TMA tile loads of A and one
 //               bulk copy of the B chunk, completing on the stage barrier;
 //   warp 1      MMA issuer: per chunk 4 MMAs (K = 16) per tile into the
 //               item's accumulator slot, commit frees the stage; the last
 //               chunk's commit hands the slot to the epilogue;
-//   warps 2-9   epilogue: two warps per TMEM lane quarter, alternate 8-slot
-//               column chunks.
+//   warps 2-17  epilogue: four warps per TMEM lane quarter; each reads its
+//               (at most two) 8-slot column chunks out of tensor memory,
+//               releases the slot, then rotates and stores.
 // Two accumulator slots of 256 columns (R tiles x N columns each) let the
 // MMAs of one item run while the epilogue drains the previous one.
 //
@@ -43,6 +49,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -139,8 +146,9 @@ struct TcCursor {
   int32_t cur[kTcMaxMsets];
   int32_t end[kTcMaxMsets];
   int64_t P[kTcMaxMsets];
-  __device__ void init(const TcLaunch& L, int b) {
-    for (int m = 0; m < L.nmsets; ++m) {
+  // (the lanes of a warp split the merge sets)
+  __device__ void init(const TcLaunch& L, int b, int lane) {
+    for (int m = lane; m < L.nmsets; m += 32) {
       const TcMset& M = L.ms[m];
       P[m] = (int64_t)M.R * kTcRows * L.groups[M.group].D;
       int64_t f, l;
@@ -149,20 +157,35 @@ struct TcCursor {
       end[m] = (int32_t)l;
     }
   }
-  __device__ bool next(const TcLaunch& L, int* m_out, int* t_out) {
-    int best = -1;
-    int64_t bu = 0;
-    for (int m = 0; m < L.nmsets; ++m) {
+  // The next item in input order (ties: the lower merge set), found by the
+  // whole warp: each lane scans every 32nd merge set, then a butterfly
+  // reduction; every lane returns the same item.
+  __device__ bool next(const TcLaunch& L, int lane, int* m_out, int* t_out) {
+    int64_t bu = INT64_MAX;
+    int bm = INT32_MAX;
+    for (int m = lane; m < L.nmsets; m += 32) {
       if (cur[m] >= end[m]) continue;
       const int64_t u = (int64_t)L.ms[m].a + (int64_t)cur[m] * P[m];
-      if (best < 0 || u < bu) {
-        best = m;
+      if (u < bu) {
         bu = u;
+        bm = m;
       }
     }
-    if (best < 0) return false;
-    *m_out = best;
-    *t_out = cur[best]++;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const int64_t u2 = __shfl_xor_sync(0xffffffffu, bu, o);
+      const int m2 = __shfl_xor_sync(0xffffffffu, bm, o);
+      if (u2 < bu || (u2 == bu && m2 < bm)) {
+        bu = u2;
+        bm = m2;
+      }
+    }
+    if (bm == INT32_MAX) return false;
+    *m_out = bm;
+    *t_out = cur[bm];
+    __syncwarp();
+    if (lane == 0) cur[bm]++;
+    __syncwarp();
     return true;
   }
 };
@@ -179,6 +202,11 @@ struct TcCursor {
 // of the tap's hi or lo part.
 template <int FMT>
 __global__ void __launch_bounds__(256) tc_prep_kernel(const __grid_constant__ TcLaunch L, int nb_build) {
+  if (blockIdx.x == 0) {  // the record, for the filter-bank kernel
+    const uint4* src = reinterpret_cast<const uint4*>(&L);
+    uint4* dst = reinterpret_cast<uint4*>(L.rec_out);
+    for (int i = (int)threadIdx.x; i < (int)(sizeof(TcLaunch) / 16); i += 256) dst[i] = src[i];
+  }
   if ((int)blockIdx.x < nb_build) {
     const int total = L.bprefix[L.nmsets];
     for (int p = (int)blockIdx.x * 256 + (int)threadIdx.x; p < total; p += nb_build * 256) {
@@ -289,11 +317,67 @@ __device__ __noinline__ void tc_fix_exact(const TcLaunch& L, int slot, int64_t j
   *dst = rotate_apply(er, *dst, B);
 }
 
+// Row stride D' of the merge set that holds slot s.
+__device__ __forceinline__ int64_t tc_slot_stride(const TcLaunch& L, int s) {
+  for (int m = 0; m < L.nmsets; ++m)
+    if (s >= L.ms[m].slot0 && s < L.ms[m].slot0 + L.ms[m].NS) return L.groups[L.ms[m].group].D;
+  return 0;
+}
+
+// Whether the filter-bank epilogue rotates slot S's rows itself (its fast
+// path); when not, every row of the slot was stored unrotated.
+__device__ __forceinline__ bool tc_slot_fast(const TcLaunch& L, const NcoConst& nc, int64_t Dp, int T) {
+  return !L.exact_all && nc.rollover < 0x80000000u && (int64_t)31 * Dp + T < (int64_t)nc.rollover;
+}
+
+// Exact rotation of the rows that the filter-bank kernel stored unrotated:
+// windows that straddle the NCO rollover (the phase restarts inside the
+// window, so the product splits into the taps before and after it), or every
+// row of a slot whose rollover is too short (or too long) for the epilogue's
+// 32-bit counters.  Blocks (slot, y): the gridDim.y blocks of a slot take its
+// rollover points (or its rows) in turn.  Runs after the filter-bank launch
+// on the same stream.
+__global__ void __launch_bounds__(128) tc_fix_kernel(const __grid_constant__ TcLaunch L) {
+  const int s = blockIdx.x;
+  if (s >= L.nslots) return;
+  const TcSlot& S = L.slots[s];
+  if (S.J <= 0 || S.T == 0) return;
+  const NcoConst nc = L.nco[S.ch];
+  if (!nc.enabled || nc.omega64 == 0 || nc.rollover == 0) return;
+  const int64_t Dp = tc_slot_stride(L, s);
+  if (Dp <= 0) return;
+  float2* out = reinterpret_cast<float2*>(S.out);
+  const int64_t J = S.J, T = S.T, R = nc.rollover;
+  const int64_t t0 = (int64_t)blockIdx.y * blockDim.x + threadIdx.x, tstep = (int64_t)gridDim.y * blockDim.x;
+  if (!tc_slot_fast(L, nc, Dp, (int)T)) {
+    for (int64_t j = t0; j < J; j += tstep) tc_fix_exact(L, s, j, Dp, out + (uint64_t)S.U * (uint64_t)j);
+    return;
+  }
+  // rollover points n (block relative): (nco_base + n) mod R == 0; row j's
+  // window [w0 + j D', w0 + j D' + T - 1] straddles n when it holds n - 1 and n
+  const int64_t w0 = S.w0;
+  const int64_t base = L.nco_base[S.ch];
+  const int64_t first = w0 + 1;                            // smallest n a window can straddle
+  const int64_t last = w0 + (J - 1) * Dp + T - 1;          // largest
+  int64_t r0 = (base + first) % R;
+  if (r0 < 0) r0 += R;
+  const int64_t n0 = first + (r0 == 0 ? 0 : R - r0);
+  for (int64_t n = n0 + t0 * R; n <= last; n += tstep * R) {
+    // rows with n - T + 1 <= w0 + j D' <= n - 1
+    const int64_t lo = n - T + 1 - w0, hi = n - 1 - w0;
+    int64_t j0 = lo <= 0 ? 0 : (lo + Dp - 1) / Dp;
+    int64_t j1 = hi < 0 ? -1 : hi / Dp;
+    if (j1 > J - 1) j1 = J - 1;
+    for (int64_t j = j0; j <= j1; ++j) tc_fix_exact(L, s, j, Dp, out + (uint64_t)S.U * (uint64_t)j);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // the filter-bank kernel
 // ---------------------------------------------------------------------------
 template <int FMT>
-__global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_constant__ TcLaunch L) {
+__global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_constant__ TcFilterParams P) {
+  const TcLaunch& L = *P.rec;
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[kTcMaxStages];
   __shared__ __align__(8) uint64_t empty_bar[kTcMaxStages];
@@ -351,7 +435,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
       if (nc.enabled) {
         // fast path: row counters (P0 + lane D) stay below 2 R < 2^32 with one
         // conditional subtraction; otherwise every output goes exact (R = 0)
-        const bool fast = nc.rollover < 0x80000000u && (int64_t)31 * D + S.T < (int64_t)nc.rollover;
+        const bool fast = tc_slot_fast(L, nc, D, S.T);
         e.om = nc.omega64;
         e.fm = nc.fastmod;
         e.x0 = (int64_t)L.nco_base[S.ch] + S.w0;
@@ -367,60 +451,71 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    if (lane == 0) {
-      TcCursor& cur = cursor;
-      cur.init(L, blockIdx.x);
-      int64_t ci = 0;  // chunks issued
-      int64_t k = 0;   // items announced
-      bool failed = false;
-      int m, t;
-      while (!L.hold && !failed) {
-        const bool more = cur.next(L, &m, &t);
-        // announce item k (or the end of the sequence) with its first stage
-        {
-          const int s = (int)(ci % stages);
-          const int64_t kk = ci / stages;
-          if (kk > 0 && !tc::mbar_wait_bounded(&empty_bar[s], (uint32_t)((kk - 1) & 1), poll)) {
-            failed = true;
-            break;
-          }
-          ring[k % kTcRing] = make_int2(more ? m : -1, more ? t : 0);
-          ++k;
-          if (!more) {
-            tc::mbar_arrive(&full_bar[s]);  // no copies: the consumers read the end marker
-            ++ci;
-            break;
-          }
+    // the whole warp walks the item sequence; lane 0 takes the waits (their
+    // outcome is shared with the warp) and issues the copies
+    TcCursor& cur = cursor;
+    cur.init(L, blockIdx.x, lane);
+    __syncwarp();
+    auto wait0 = [&](uint64_t* bar, uint32_t parity) {
+      bool ok = true;
+      if (lane == 0) ok = tc::mbar_wait_bounded(bar, parity, poll);
+      return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    };
+    int64_t ci = 0;  // chunks issued
+    int64_t k = 0;   // items announced
+    bool failed = false;
+    int m = 0, t = 0;
+    while (!L.hold && !failed) {
+      const bool more = cur.next(L, lane, &m, &t);
+      // announce item k (or the end of the sequence) with its first stage
+      {
+        const int s = (int)(ci % stages);
+        const int64_t kk = ci / stages;
+        if (kk > 0 && !wait0(&empty_bar[s], (uint32_t)((kk - 1) & 1))) {
+          failed = true;
+          break;
         }
-        const TcMset& M = L.ms[m];
-        const int D = L.groups[M.group].D;
-        const CUtensorMap* map = &L.maps[M.group];
-        const int R = M.R;
-        const uint32_t bbytes = (uint32_t)(4 * M.NS * 128);
-        const uint32_t tx = (uint32_t)R * kTcTileBytes + bbytes;
-        const int32_t x0 = 4 * (M.a % D);
-        const int32_t y0 = t * R * kTcRows + M.a / D;
-        const uint8_t* bsrc = L.bbuf + M.b;
-        for (int c = 0; c < M.nchunks; ++c, ++ci) {
-          const int s = (int)(ci % stages);
-          const int64_t kk = ci / stages;
-          // (the first chunk's stage was claimed with the announcement)
-          if (c > 0 && kk > 0 && !tc::mbar_wait_bounded(&empty_bar[s], (uint32_t)((kk - 1) & 1), poll)) {
-            failed = true;
-            break;
-          }
+        if (lane == 0) ring[k % kTcRing] = make_int2(more ? m : -1, more ? t : 0);
+        ++k;
+        if (!more) {
+          if (lane == 0) tc::mbar_arrive(&full_bar[s]);  // no copies: the consumers read the end marker
+          ++ci;
+          break;
+        }
+      }
+      const TcMset& M = L.ms[m];
+      const int D = L.groups[M.group].D;
+      const CUtensorMap* map = &P.maps[M.group];
+      const int R = M.R;
+      const uint32_t bbytes = (uint32_t)(4 * M.NS * 128);
+      const uint32_t tx = (uint32_t)R * kTcTileBytes + bbytes;
+      const int32_t x0 = 4 * (M.a % D);
+      const int32_t y0 = t * R * kTcRows + M.a / D;
+      const uint8_t* bsrc = L.bbuf + M.b;
+      const int nchunks = M.nchunks;
+      for (int c = 0; c < nchunks; ++c, ++ci) {
+        const int s = (int)(ci % stages);
+        const int64_t kk = ci / stages;
+        // (the first chunk's stage was claimed with the announcement)
+        if (c > 0 && kk > 0 && !wait0(&empty_bar[s], (uint32_t)((kk - 1) & 1))) {
+          failed = true;
+          break;
+        }
+        if (lane == 0) {
           const uint32_t st = sbase + (uint32_t)s * (uint32_t)L.stage_bytes;
           const uint32_t fb = tc::smem_u32(&full_bar[s]);
           mbar_expect_tx(&full_bar[s], tx);
-          for (int r = 0; r < R; ++r) tma_load_2d(st + (uint32_t)r * kTcTileBytes, map, x0 + 64 * c, y0 + r * kTcRows, fb);
+          for (int r = 0; r < R; ++r)
+            tma_load_2d(st + (uint32_t)r * kTcTileBytes, map, x0 + 64 * c, y0 + r * kTcRows, fb);
           bulk_load(st + (uint32_t)R * kTcTileBytes, bsrc + (size_t)c * bbytes, bbytes, fb);
         }
+        __syncwarp();
       }
-      // every copy issued lands before the CTA can exit
-      for (int64_t i = (ci > stages ? ci - stages : 0); i < ci; ++i)
-        if (!tc::mbar_wait_bounded(&full_bar[i % stages], (uint32_t)((i / stages) & 1), poll)) failed = true;
-      if (failed) atomicExch(L.err, 1);
     }
+    // every copy issued lands before the CTA can exit
+    for (int64_t i = (ci > stages ? ci - stages : 0); i < ci; ++i)
+      if (!wait0(&full_bar[i % stages], (uint32_t)((i / stages) & 1))) failed = true;
+    if (failed && lane == 0) atomicExch(L.err, 1);
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     int64_t ci = 0;
@@ -510,14 +605,40 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
       const int R = M.R, NS = M.NS, nch = NS >> 3;
       const int64_t D = L.groups[M.group].D;
       const uint32_t laneD = (uint32_t)lane * (uint32_t)D;
-      for (int idx = h; idx < R * nch; idx += 4) {
+      // every column chunk this warp owns (at most two: R * NS <= 64) is read
+      // out of tensor memory first and the accumulator slot released, so the
+      // MMAs of a later item run while this warp rotates and stores
+      const int n_own = (R * nch - h + 3) >> 2;  // chunks h, h + 4 (0, 1 or 2)
+      float ya[16], yb[16];                      // (hi + lo) sums of the two chunks
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (u < n_own) {
+          const int idx = h + 4 * u;
+          const int r = idx / nch, cc = idx - r * nch;
+          const uint32_t col = tbase + lane_off + (uint32_t)a * 256u + (uint32_t)(r * (256 / R) + 16 * cc);
+          uint32_t vh[16], vl[16];
+          tc::tmem_ld16(col, vh);
+          tc::tmem_ld16(col + (uint32_t)(2 * NS), vl);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) (u == 0 ? ya : yb)[i] = __uint_as_float(vh[i]) + __uint_as_float(vl[i]);
+        }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&acc_empty[a]);
+      // one copy of the chunk code (kept small: the warps of every role share
+      // the SM's instruction cache); the second chunk moves into ya after the first
+#pragma unroll 1
+      for (int u = 0; u < n_own; ++u) {
+        if (u > 0) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) ya[i] = yb[i];
+        }
+        const int idx = h + 4 * u;
         const int r = idx / nch, cc = idx - r * nch;
         const int64_t row0 = ((int64_t)t * R + r) * kTcRows + q * 32;  // row of lane 0
         const int64_t j = row0 + lane;
-        const uint32_t col = tbase + lane_off + (uint32_t)a * 256u + (uint32_t)(r * (256 / R) + 16 * cc);
-        uint32_t vh[16], vl[16];
-        tc::tmem_ld16(col, vh);
-        tc::tmem_ld16(col + (uint32_t)(2 * NS), vl);
         const TcEpiSlot* E8 = etab + M.slot0 + cc * 8;
         // NCO counter of lane 0's window start for slot e (lane e computes it):
         // (x0 + row0 D) mod R, once per chunk; 0 <= x0 + row0 D < 2^32 or
@@ -531,15 +652,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
                        : (uint32_t)__umul64hi(E.fm * (uint64_t)(uint32_t)v, (uint64_t)E.R);
           }
         }
-        tc::tmem_wait_ld();
-        uint32_t slow = 0;
         float2 o[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
           const TcEpiSlot& E = E8[e];
           const uint32_t P0 = __shfl_sync(0xffffffffu, p0, e);
-          const float2 y0 = make_float2(__uint_as_float(vh[2 * e]) + __uint_as_float(vl[2 * e]),
-                                        __uint_as_float(vh[2 * e + 1]) + __uint_as_float(vl[2 * e + 1]));
+          const float2 y0 = make_float2(ya[2 * e], ya[2 * e + 1]);
           uint32_t pc = P0 + laneD;
           pc = pc >= E.R ? pc - E.R : pc;
           const bool fast = pc + E.Tm1 < E.R || E.om == 0;
@@ -548,8 +666,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
           float sn, cs;
           __sincosf((float)(int32_t)turns * 1.4629180792671596e-09f, &sn, &cs);  // 2 pi / 2^32
           const float2 y = cmul_nco(y0, make_float2(cs, sn));
-          o[e] = fast ? y : y0;
-          slow |= (fast || j >= E.J) ? 0u : (1u << e);
+          o[e] = fast ? y : y0;  // windows across the NCO rollover: unrotated, for tc_fix_kernel
         }
         // stores: a slot and the next one holding the same channel's next
         // output go out as one 16-byte store (contiguous across the lanes
@@ -567,16 +684,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
             if (v1) __stcs(reinterpret_cast<float2*>(E1.out) + (uint64_t)E1.U * (uint64_t)j, o[e + 1]);
           }
         }
-        while (slow) {  // rare: windows across the NCO rollover
-          const int e = __ffs(slow) - 1;
-          slow &= slow - 1;
-          const TcEpiSlot& E = E8[e];
-          tc_fix_exact(L, E.slot, j, D, reinterpret_cast<float2*>(E.out) + (uint64_t)E.U * (uint64_t)j);
-        }
       }
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&acc_empty[a]);
     }
     if (failed && lane == 0) atomicExch(L.err, 1);
   }
@@ -612,11 +720,13 @@ void PolyEngine::free_tc() {
   if (d_ctab_) cudaFree(d_ctab_);
   if (d_xhl_) cudaFree(d_xhl_);
   if (d_bbuf_) cudaFree(d_bbuf_);
+  if (d_tcrec_) cudaFree(d_tcrec_);
   if (h_err_) cudaFreeHost(h_err_);
   d_ctaps_ = nullptr;
   d_ctab_ = nullptr;
   d_xhl_ = nullptr;
   d_bbuf_ = nullptr;
+  d_tcrec_ = nullptr;
   h_err_ = nullptr;
   d_err_ = nullptr;
   xhl_cap_ = 0;
@@ -665,6 +775,7 @@ int PolyEngine::build_tc(int fmt) {
   for (size_t c = 0; c < chans_.size(); ++c) tab[c] = d_ctaps_ + off[c];
   if (err == cudaSuccess) err = cudaMalloc(&d_ctab_, tab.size() * sizeof(float2*));
   if (err == cudaSuccess) err = cudaMemcpy(d_ctab_, tab.data(), tab.size() * sizeof(float2*), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMalloc(&d_tcrec_, sizeof(TcLaunch));
   if (err == cudaSuccess) err = cudaHostAlloc(&h_err_, sizeof(int), cudaHostAllocMapped);
   if (err == cudaSuccess) {
     *h_err_ = 0;
@@ -802,6 +913,7 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     L.xhl = d_xhl_;
     L.bbuf = d_bbuf_;
     L.err = d_err_;
+    L.rec_out = d_tcrec_;
     L.N = (int64_t)n;
     L.Lc = plan.Lc;
     L.xhl_n = xhl_need;
@@ -814,6 +926,7 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     L.nslots = (int32_t)plan.slots.size();
     L.poll = tc_poll_;
     L.hold = tc_hold_;
+    L.exact_all = tc_exact_all_;
     for (size_t c = 0; c < chans_.size(); ++c) {
       const uint32_t R = chans_[c].nco.rollover;
       L.nco_base[c] = R ? (uint32_t)(abs0_ % R) : 0u;
@@ -859,8 +972,30 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, plan.smem);
     if (e != cudaSuccess) return cuda_status(e);
     if (kprof_) cudaEventRecord(kprof_event(), stream);
-    kern<<<(unsigned)plan.G, kTcThreads, (size_t)plan.smem, stream>>>(L);
+    static thread_local TcFilterParams FP;
+    std::memcpy(FP.maps, L.maps, sizeof(FP.maps));
+    FP.rec = d_tcrec_;
+    kern<<<(unsigned)plan.G, kTcThreads, (size_t)plan.smem, stream>>>(FP);
     if (kprof_) cudaEventRecord(kprof_event(), stream);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+    launches_last_++;
+    // exact pass: blocks per slot for the most rows (or rollover points) a
+    // slot of this launch has to fix
+    int64_t work = 1;
+    for (size_t si = 0; si < plan.slots.size(); ++si) {
+      const TcSlot& S = plan.slots[si];
+      if (S.J <= 0) continue;
+      const NcoConst& nc = chans_[S.ch].nco;
+      if (!nc.enabled || nc.omega64 == 0 || nc.rollover == 0) continue;
+      int64_t Dp = 0;
+      for (const TcMset& m : plan.ms)
+        if ((int)si >= m.slot0 && (int)si < m.slot0 + m.NS) Dp = plan.groups[m.group].D;
+      const bool fast = !tc_exact_all_ && nc.rollover < 0x80000000u && 31 * Dp + S.T < (int64_t)nc.rollover;
+      work = std::max<int64_t>(work, fast ? ((int64_t)S.J * Dp + S.T) / nc.rollover + 1 : (int64_t)S.J);
+    }
+    const unsigned fix_y = (unsigned)std::min<int64_t>(4096, (work + 511) / 512);
+    tc_fix_kernel<<<dim3((unsigned)plan.slots.size(), fix_y), 128, 0, stream>>>(L);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;

@@ -113,12 +113,14 @@ struct TcLaunch {
   uint2* xhl;                        // [history | block | zeros] as {hi, lo} 16-bit parts (prep writes it)
   uint8_t* bbuf;                     // B images of the merge sets (prep writes them)
   int* err;                          // bounded-wait failures (mapped host memory)
+  TcLaunch* rec_out;                 // device copy of this record (the prep kernel writes it)
   int64_t N;                         // block samples
   int64_t Lc;                        // samples of the time range each CTA owns
   int64_t xhl_n;                     // samples of xhl the prep writes
   int32_t H, G, nmsets, ngroups, stages, stage_bytes, nslots;
   uint32_t poll;                     // polls before a wait gives up (each suspends up to ~2 us)
   int32_t hold;                      // test hook: the producer issues nothing (every wait runs out)
+  int32_t exact_all;                 // test hook: every output takes the exact rotation pass
   int32_t bprefix[kTcMaxMsets + 1];  // 16-byte pieces of the B images before merge set m
   TcGroup groups[kTcMaxGroups];
   TcMset ms[kTcMaxMsets];
@@ -127,6 +129,15 @@ struct TcLaunch {
 };
 
 static_assert(sizeof(TcLaunch) <= 32764, "tensor-core launch must fit the kernel parameter block");
+static_assert(sizeof(TcLaunch) % 16 == 0, "tensor-core launch record is copied in 16-byte pieces");
+
+// Parameters of the filter-bank kernel: the tensor maps (TMA reads them from
+// the parameter space) and the launch record, which the prep kernel copied
+// into device memory -- a 2 KB parameter block instead of the 32 KB record.
+struct TcFilterParams {
+  CUtensorMap maps[kTcMaxGroups];
+  const TcLaunch* rec;
+};
 
 // CUDA error -> status, remembering the CUDA code for fdsp_last_cuda_error().
 int cuda_status(cudaError_t e);
@@ -248,6 +259,7 @@ class PolyEngine {
   // summed milliseconds and the launch count since profiling was enabled.
   void set_profile(bool on);
   int read_profile(double* ms, uint32_t* launches);
+  void set_tc_exact_all(int on) { tc_exact_all_ = on; }
   void set_tc_wait(uint32_t polls, int hold) {
     tc_poll_ = polls ? polls : 1u;
     tc_hold_ = hold;
@@ -291,11 +303,13 @@ class PolyEngine {
   uint2* d_xhl_ = nullptr;             // scratch: split input of the current apply
   size_t xhl_cap_ = 0;                 // samples
   uint8_t* d_bbuf_ = nullptr;          // scratch: B images of the current apply
+  TcLaunch* d_tcrec_ = nullptr;        // device copy of the current tensor-core launch record
   size_t bbuf_cap_ = 0;
   int* h_err_ = nullptr;               // bounded-wait failures, mapped host memory
   int* d_err_ = nullptr;               // its device address
   uint32_t tc_poll_ = 1u << 20;
   int tc_hold_ = 0;
+  int tc_exact_all_ = 0;
   int num_sms_ = 0;
 
   uint32_t fs_ = 0;

@@ -43,8 +43,9 @@ def test_fm_chain_matches_oracle_and_recovers_audio():
 def test_fm_chain_tensor_core_vs_fp64(mode):
     """The same chain with the 4095-tap resampler on the tensor cores (split
     precision, FP32 accumulation, K chunked over 256 chunks of 16 taps):
-    streamed in 2^16-sample blocks, every block's resampler output >= 60 dB
-    SNR against the FP64 oracle, counts exact, the tensor-core form really
+    streamed in 2^16-sample blocks, every block's resampler output above
+    the form's SNR floor against the FP64 oracle (lowest block measured on
+    a GB300: fp16x3 96.1 dB, bf16x3 95.5 dB; floor 3 dB below), counts exact, the tensor-core form really
     ran, and the recovered audio keeps its SNR within 0.5 dB of the FP64
     chain's."""
     torch = pytest.importorskip("torch")
@@ -72,5 +73,5 @@ def test_fm_chain_tensor_core_vs_fp64(mode):
     snr_tc = audio_snr_db(np.concatenate(audio), fs / 10, tones)
     snr_64 = audio_snr_db(a64, fs / 10, tones)
     print(f"{mode}: worst block SNR vs FP64 {worst:.1f} dB; audio SNR {snr_tc:.2f} dB (FP64 chain {snr_64:.2f} dB)")
-    assert worst >= 60.0, worst
+    assert worst >= {"fp16x3": 93.0, "bf16x3": 92.0}[mode], worst
     assert abs(snr_tc - snr_64) <= 0.5

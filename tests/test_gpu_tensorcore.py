@@ -74,6 +74,32 @@ def test_tc_rollover_straddles_and_matches_fp32_path():
                 assert snr_db(ya, yc) >= 100.0
 
 
+def test_tc_exact_pass_for_every_output():
+    """The exact rotation pass (tc_fix_kernel) over every output of a slot --
+    the path of slots whose row stride spans more than the NCO rollover (31
+    rows of D' samples >= R), forced here by the test hook on an ordinary
+    plan -- and over the straddling windows alone, within the tensor-core
+    bound of the FP64 oracle and equal to each other within FP32 rounding."""
+    fs = 1000000
+    chans = [dict(freq_shift_in_hz=f, up_rate=u, down_rate=d, coeffs=_rand(u * t, 50 + i, 0.05).real.astype(np.complex64))
+             for i, (f, u, d, t) in enumerate([(100000, 1, 4, 64), (-100000, 3, 8, 40), (12345, 2, 25, 33),
+                                               (0, 1, 4, 20)])]
+    x = _rand(300000, 51)
+    a = F.MultiRateChannelizerCuda(fs, chans)
+    b = F.MultiRateChannelizerCuda(fs, chans)
+    for g in (a, b):
+        g.set_precision("fp16x3")
+    b.set_tc_exact_all(True)
+    o64 = O.Channelizer(fs, chans, precision="f64")
+    for i, j in [(0, 4001), (4001, 150000), (150000, 300000)]:
+        for ya, yb, yc in zip(a.apply(x[i:j]), b.apply(x[i:j]), o64.apply(x[i:j])):
+            assert ya.size == yb.size == yc.size
+            if yc.size > 8:
+                assert snr_db(yb, yc) >= SNR_MIN_DB, snr_db(yb, yc)
+                assert snr_db(yb, ya) >= 110.0, snr_db(yb, ya)
+    assert b.tc_groups() == a.tc_groups() >= 1
+
+
 @pytest.mark.parametrize("split", [1, 2, 4])
 def test_tc_row_split_matches_fp64(split):
     """Row split (rows j = S i + b of a group run as S output streams whose

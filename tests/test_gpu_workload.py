@@ -5,7 +5,8 @@ combine an oracle check on a prefix with size-independent properties:
   * output counts equal the reference loop's counts (closed form, bit-exact);
   * streaming the block in 2^16-sample pieces equals one-shot processing;
   * scaling the input by 2 scales every output by exactly 2 (bit-exact);
-  * the tensor-core forms stay >= 60 dB SNR from the plain FP32 form;
+  * the tensor-core forms stay above a per-form SNR floor (TC_FLOOR_DB) from
+    the plain FP32 form;
   * on a prefix, every channel matches the oracle (FP32 <= 1e-5 relative RMS,
     tensor cores above a per-form SNR floor against the FP64 oracle).
 """
@@ -19,6 +20,12 @@ from tests.golden_io import rel_rms, snr_db
 
 pytestmark = pytest.mark.gpu
 FS = 61440000
+
+# Per-form SNR floors (dB) of the tensor-core forms on this workload: the
+# lowest channel measured on a GB300 (fp16x3 116.3-117.4 dB, bf16x3
+# 106.2-106.5 dB, against the FP64 oracle and against the FP32 form) minus
+# a 3 dB margin.
+TC_FLOOR_DB = {"fp16x3": 113.0, "bf16x3": 103.0}
 
 
 def test_plan_prefix_vs_oracle_all_channels():
@@ -44,7 +51,7 @@ def test_plan_prefix_vs_oracle_all_channels():
                 assert rel_rms(y, a) <= 1e-5
             snrs.append(snr_db(y, b))
         res[mode] = (min(snrs), float(np.median(snrs)))
-        assert min(snrs) >= 60.0, (mode, min(snrs))
+        assert min(snrs) >= TC_FLOOR_DB.get(mode, 60.0), (mode, min(snrs))
     print("SNR vs FP64 oracle over 256 channels (min, median dB):", res)
 
 
@@ -101,7 +108,7 @@ def test_full_size_tensor_core_vs_fp32(full, mode):
         sig = torch.linalg.vector_norm(a) ** 2
         worst = min(worst, float(10 * torch.log10(sig / err)))
     print(f"{mode}: worst channel SNR vs plain FP32 over 2^26 samples: {worst:.1f} dB")
-    assert worst >= 60.0
+    assert worst >= TC_FLOOR_DB[mode], (mode, worst)
     # linearity in scale: exact for BF16 (its exponent range keeps every lo
     # part normal); FP16 lo parts of tiny samples are subnormal, so scaling
     # moves their rounding -- there the bound is 100 dB
@@ -114,9 +121,6 @@ def test_full_size_tensor_core_vs_fp32(full, mode):
             assert float(10 * torch.log10(torch.linalg.vector_norm(b) ** 2 / err)) >= 100.0
 
 
-# Per-form SNR floors against the FP64 oracle (dB): the lowest channel
-# measured on the GB300 minus a 3 dB margin.
-TC_FLOOR_DB = {"fp16x3": 60.0, "bf16x3": 60.0}
 
 
 @pytest.mark.parametrize("mode", ["fp16x3", "bf16x3"])
