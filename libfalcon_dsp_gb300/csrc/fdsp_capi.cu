@@ -33,7 +33,70 @@ struct fdsp_channelizer {
   PolyEngine eng;
   DevBuf in;
   std::vector<DevBuf> out;
+  // apply_host: device-to-host copies on their own stream, each group's
+  // started as soon as the launches that write it are enqueued
+  cudaStream_t copy = nullptr;
+  std::vector<cudaEvent_t> ev;
+  size_t ev_used = 0;
+  fdsp_cf32* const* h_out = nullptr;
+  const float2* const* d_out = nullptr;
+  const uint64_t* n_out = nullptr;
+  int copy_err = 0;
+  ~fdsp_channelizer() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (copy) cudaStreamDestroy(copy);
+  }
 };
+
+namespace {
+cudaEvent_t next_event(fdsp_channelizer* h) {
+  if (h->ev_used == h->ev.size()) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    h->ev.push_back(e);
+  }
+  return h->ev[h->ev_used++];
+}
+
+// PolyEngine completion hook: the listed channels' outputs are complete once
+// `stream` reaches this point; copy them back on the copy stream.
+void channelizer_copy_back(void* ctx, const int* chans, int count, cudaStream_t stream) {
+  fdsp_channelizer* h = static_cast<fdsp_channelizer*>(ctx);
+  cudaEvent_t e = next_event(h);
+  if (!e || cudaEventRecord(e, stream) != cudaSuccess || cudaStreamWaitEvent(h->copy, e, 0) != cudaSuccess) {
+    h->copy_err = 1;
+    return;
+  }
+  for (int i = 0; i < count; ++i) {
+    const int c = chans[i];
+    if (h->n_out[c] && cudaMemcpyAsync(h->h_out[c], h->d_out[c], h->n_out[c] * sizeof(float2),
+                                       cudaMemcpyDeviceToHost, h->copy) != cudaSuccess)
+      h->copy_err = 1;
+  }
+}
+
+// apply (float or int16 input) with the outputs copied back group by group
+// while the later groups compute; the caller's stream waits for every copy.
+template <class ApplyFn>
+int apply_with_copy_back(fdsp_channelizer* h, fdsp_cf32* const* h_out, float2* const* dptr, uint64_t* n_out,
+                         cudaStream_t s, ApplyFn&& fn) {
+  if (!h->copy) FDSP_TRY(cuda_status(cudaStreamCreateWithFlags(&h->copy, cudaStreamNonBlocking)));
+  h->ev_used = 0;
+  h->copy_err = 0;
+  h->h_out = h_out;
+  h->d_out = dptr;
+  h->n_out = n_out;
+  h->eng.set_done_hook(channelizer_copy_back, h);
+  const int st = fn();
+  h->eng.set_done_hook(nullptr, nullptr);
+  cudaEvent_t e = next_event(h);
+  if (!e) return FDSP_ERR_CUDA;
+  FDSP_TRY(cuda_status(cudaEventRecord(e, h->copy)));
+  FDSP_TRY(cuda_status(cudaStreamWaitEvent(s, e, 0)));
+  if (st != FDSP_OK) return st;
+  return h->copy_err ? FDSP_ERR_CUDA : FDSP_OK;
+}
+}  // namespace
 
 struct fdsp_resampler {
   PolyEngine eng;
@@ -335,12 +398,9 @@ int fdsp_channelizer_apply_host(fdsp_channelizer* h, const fdsp_cf32* h_in, uint
     dptr[c] = static_cast<float2*>(h->out[c].p);
   }
   if (n_in) FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * sizeof(float2), cudaMemcpyHostToDevice, s)));
-  FDSP_TRY(h->eng.apply(static_cast<const float2*>(h->in.p), n_in, dptr.data(), nullptr, n_out, s));
-  for (uint32_t c = 0; c < nch; ++c) {
-    if (n_out[c])
-      FDSP_TRY(cuda_status(
-          cudaMemcpyAsync(h_out[c], dptr[c], n_out[c] * sizeof(float2), cudaMemcpyDeviceToHost, s)));
-  }
+  FDSP_TRY(apply_with_copy_back(h, h_out, dptr.data(), n_out, s, [&] {
+    return h->eng.apply(static_cast<const float2*>(h->in.p), n_in, dptr.data(), nullptr, n_out, s);
+  }));
   return engine_status(h->eng, s);
 }
 
@@ -364,12 +424,9 @@ int fdsp_channelizer_apply_ci16_host(fdsp_channelizer* h, const int16_t* h_in, u
   }
   if (n_in)
     FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * 2 * sizeof(int16_t), cudaMemcpyHostToDevice, s)));
-  FDSP_TRY(h->eng.apply_ci16(static_cast<const int16_t*>(h->in.p), n_in, dptr.data(), nullptr, n_out, s));
-  for (uint32_t c = 0; c < nch; ++c) {
-    if (n_out[c])
-      FDSP_TRY(cuda_status(
-          cudaMemcpyAsync(h_out[c], dptr[c], n_out[c] * sizeof(float2), cudaMemcpyDeviceToHost, s)));
-  }
+  FDSP_TRY(apply_with_copy_back(h, h_out, dptr.data(), n_out, s, [&] {
+    return h->eng.apply_ci16(static_cast<const int16_t*>(h->in.p), n_in, dptr.data(), nullptr, n_out, s);
+  }));
   return engine_status(h->eng, s);
 }
 

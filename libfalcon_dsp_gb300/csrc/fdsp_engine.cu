@@ -707,6 +707,15 @@ int PolyEngine::set_precision(int mode) {
   return FDSP_OK;
 }
 
+void PolyEngine::notify_done(const std::vector<int>& egroups, cudaStream_t stream) {
+  if (!done_fn_ || egroups.empty()) return;
+  std::vector<int> ch;
+  for (int eg : egroups)
+    for (const EngineClass& k : classes_)
+      if (k.down == groups_[eg].D && k.M > 0) ch.insert(ch.end(), k.chans.begin(), k.chans.end());
+  if (!ch.empty()) done_fn_(done_ctx_, ch.data(), (int)ch.size(), stream);
+}
+
 void PolyEngine::set_graph(bool on) {
   use_graph_ = on;
   graph_replays_ = 0;
@@ -992,6 +1001,11 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
         e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_status(e);
         launches_last_++;
+        if (done_fn_) {
+          std::vector<int> egs;
+          for (int i = first; i < nm; ++i) egs.push_back(group_of_d_[L.groups[L.fuse_map[i]].D]);
+          notify_done(egs, stream);
+        }
       }
       for (int gi = 0; gi < ng; ++gi) on_tc[gi] = 1;  // nothing left for the per-group loop
     }
@@ -1018,6 +1032,7 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     if (!prof_ev_.empty()) cudaEventRecord(prof_ev_[2 * eg + 1], stream);
+    if (done_fn_) notify_done(std::vector<int>(1, eg), stream);
   }
   if (H_ > 0) {
     hist_update_kernel<<<(H_ + 255) / 256, 256, 0, stream>>>(d_hist_[hist_cur_], in16_ ? nullptr : d_in, in16_,
@@ -1054,7 +1069,7 @@ int PolyEngine::apply(const float2* d_in, uint64_t n, float2* const* out, const 
   }
   if (n == 0) return FDSP_OK;
   cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
-  const bool graph = use_graph_ && !kprof_ && stream != nullptr &&
+  const bool graph = use_graph_ && !kprof_ && !done_fn_ && stream != nullptr &&
                      cudaStreamIsCapturing(stream, &capturing) == cudaSuccess &&
                      capturing == cudaStreamCaptureStatusNone;
   if (graph) {

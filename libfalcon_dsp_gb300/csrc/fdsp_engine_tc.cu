@@ -147,10 +147,10 @@ struct TcCursor {
   int32_t end[kTcMaxMsets];
   int64_t P[kTcMaxMsets];
   // (the lanes of a warp split the merge sets)
-  __device__ void init(const TcLaunch& L, int b, int lane) {
+  __device__ void init(const TcLaunch& L, const TcMset* ms, const TcGroup* groups, int b, int lane) {
     for (int m = lane; m < L.nmsets; m += 32) {
-      const TcMset& M = L.ms[m];
-      P[m] = (int64_t)M.R * kTcRows * L.groups[M.group].D;
+      const TcMset& M = ms[m];
+      P[m] = (int64_t)M.R * kTcRows * groups[M.group].D;
       int64_t f, l;
       tc_item_range(M.a, P[m], M.items, L.Lc, b, L.G, &f, &l);
       cur[m] = (int32_t)f;
@@ -160,12 +160,12 @@ struct TcCursor {
   // The next item in input order (ties: the lower merge set), found by the
   // whole warp: each lane scans every 32nd merge set, then a butterfly
   // reduction; every lane returns the same item.
-  __device__ bool next(const TcLaunch& L, int lane, int* m_out, int* t_out) {
+  __device__ bool next(const TcLaunch& L, const TcMset* ms, int lane, int* m_out, int* t_out) {
     int64_t bu = INT64_MAX;
     int bm = INT32_MAX;
     for (int m = lane; m < L.nmsets; m += 32) {
       if (cur[m] >= end[m]) continue;
-      const int64_t u = (int64_t)L.ms[m].a + (int64_t)cur[m] * P[m];
+      const int64_t u = (int64_t)ms[m].a + (int64_t)cur[m] * P[m];
       if (u < bu) {
         bu = u;
         bm = m;
@@ -187,6 +187,18 @@ struct TcCursor {
     if (lane == 0) cur[bm]++;
     __syncwarp();
     return true;
+  }
+};
+
+// Position in the stage ring: stage s of round r (chunk r * stages + s),
+// advanced without a division per chunk.
+struct TcRing {
+  int s = 0, r = 0;
+  __device__ __forceinline__ void next(int stages) {
+    if (++s == stages) {
+      s = 0;
+      ++r;
+    }
   }
 };
 
@@ -277,11 +289,9 @@ struct TcEpiSlot {
   int64_t x0;     // NCO counter argument of row 0's window start (base + w0, unreduced)
   uint32_t R;     // counter rollover; 0: every output takes the exact path
   int32_t J;      // rows with an output
-  uint32_t U;     // output stride
-  uint32_t Tm1;   // taps - 1
-  int32_t slot;   // index of the slot's launch record
+  uint16_t U;     // output stride
+  uint16_t Tm1;   // taps - 1
   uint32_t pair;  // 1: the next slot holds this channel's next output (one 16-byte store)
-  int32_t pad_[2];
 };
 static_assert(sizeof(TcEpiSlot) == kTcEpiSlotBytes, "epilogue slot table layout");
 
@@ -387,12 +397,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   __shared__ uint32_t tmem_base_s;
   __shared__ int2 ring[kTcRing];       // item k: (merge set, item index); merge set -1 ends the sequence
   __shared__ TcCursor cursor;
+  __shared__ TcMset s_ms[kTcMaxMsets];       // merge sets and groups of the launch (read per item)
+  __shared__ TcGroup s_groups[kTcMaxGroups];
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
   const uint32_t sbase = (tc::smem_u32(smem_raw) + 1023u) & ~1023u;
+  // launch constants in registers (L lives in device memory, and the inline
+  // PTX's memory clobbers would otherwise reload them every chunk)
   const int stages = L.stages;
   const uint32_t poll = L.poll;
+  const uint32_t stage_bytes = (uint32_t)L.stage_bytes;
+  const bool hold = L.hold != 0;
+  const uint8_t* const bbuf = L.bbuf;
 
   if (warp == 0) {
     tc::tmem_alloc(&tmem_base_s, kTmemCols);
@@ -410,6 +427,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
     tc::mbar_init(&drain_bar, 1);
     tc::mbar_fence_init();
   }
+  for (int i = tid; i < L.nmsets; i += kTcThreads) s_ms[i] = L.ms[i];
+  for (int i = tid; i < L.ngroups; i += kTcThreads) s_groups[i] = L.groups[i];
   // epilogue constants of every slot of the launch (after the stages)
   TcEpiSlot* etab =
       reinterpret_cast<TcEpiSlot*>(smem_raw + (sbase - tc::smem_u32(smem_raw)) + (size_t)stages * L.stage_bytes);
@@ -422,10 +441,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
     e.out = S.out;
     e.J = S.J;
     e.U = S.U;
-    e.slot = s;
     e.pair = S.flags & 1u;
-    e.pad_[0] = e.pad_[1] = 0;
-    e.Tm1 = S.T > 0 ? (uint32_t)S.T - 1u : 0u;
+    e.Tm1 = (uint16_t)(S.T > 0 ? S.T - 1u : 0u);
     e.om = 0;
     e.fm = 0;
     e.x0 = 0;
@@ -454,23 +471,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
     // the whole warp walks the item sequence; lane 0 takes the waits (their
     // outcome is shared with the warp) and issues the copies
     TcCursor& cur = cursor;
-    cur.init(L, blockIdx.x, lane);
+    cur.init(L, s_ms, s_groups, blockIdx.x, lane);
     __syncwarp();
     auto wait0 = [&](uint64_t* bar, uint32_t parity) {
       bool ok = true;
-      if (lane == 0) ok = tc::mbar_wait_bounded(bar, parity, poll);
+      if (lane == 0) ok = tc::mbar_wait_bounded_fast(bar, parity, poll);
       return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
     };
     int64_t ci = 0;  // chunks issued
+    TcRing rg;       // its stage and round
     int64_t k = 0;   // items announced
     bool failed = false;
     int m = 0, t = 0;
-    while (!L.hold && !failed) {
-      const bool more = cur.next(L, lane, &m, &t);
+    while (!hold && !failed) {
+      const bool more = cur.next(L, s_ms, lane, &m, &t);
       // announce item k (or the end of the sequence) with its first stage
       {
-        const int s = (int)(ci % stages);
-        const int64_t kk = ci / stages;
+        const int s = rg.s;
+        const int kk = rg.r;
         if (kk > 0 && !wait0(&empty_bar[s], (uint32_t)((kk - 1) & 1))) {
           failed = true;
           break;
@@ -480,29 +498,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
         if (!more) {
           if (lane == 0) tc::mbar_arrive(&full_bar[s]);  // no copies: the consumers read the end marker
           ++ci;
+          rg.next(stages);
           break;
         }
       }
-      const TcMset& M = L.ms[m];
-      const int D = L.groups[M.group].D;
+      const TcMset& M = s_ms[m];
+      const int D = s_groups[M.group].D;
       const CUtensorMap* map = &P.maps[M.group];
       const int R = M.R;
       const uint32_t bbytes = (uint32_t)(4 * M.NS * 128);
       const uint32_t tx = (uint32_t)R * kTcTileBytes + bbytes;
       const int32_t x0 = 4 * (M.a % D);
       const int32_t y0 = t * R * kTcRows + M.a / D;
-      const uint8_t* bsrc = L.bbuf + M.b;
+      const uint8_t* bsrc = bbuf + M.b;
       const int nchunks = M.nchunks;
-      for (int c = 0; c < nchunks; ++c, ++ci) {
-        const int s = (int)(ci % stages);
-        const int64_t kk = ci / stages;
+      for (int c = 0; c < nchunks; ++c, ++ci, rg.next(stages)) {
+        const int s = rg.s;
+        const int kk = rg.r;
         // (the first chunk's stage was claimed with the announcement)
         if (c > 0 && kk > 0 && !wait0(&empty_bar[s], (uint32_t)((kk - 1) & 1))) {
           failed = true;
           break;
         }
         if (lane == 0) {
-          const uint32_t st = sbase + (uint32_t)s * (uint32_t)L.stage_bytes;
+          const uint32_t st = sbase + (uint32_t)s * stage_bytes;
           const uint32_t fb = tc::smem_u32(&full_bar[s]);
           mbar_expect_tx(&full_bar[s], tx);
           for (int r = 0; r < R; ++r)
@@ -519,19 +538,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     int64_t ci = 0;
+    TcRing rg;
     int k = 0;
     bool failed = false, issued = false;
     // every wait is taken by lane 0 and its outcome shared with the warp
     auto wait_warp = [&](uint64_t* bar, uint32_t parity) {
       bool ok = true;
-      if (lane == 0) ok = tc::mbar_wait_bounded(bar, parity, poll);
+      if (lane == 0) ok = tc::mbar_wait_bounded_fast(bar, parity, poll);
       ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
       tc::fence_after_sync();
       return ok;
     };
     while (true) {
       // the first stage of item k also announces it (ring entry k)
-      if (!wait_warp(&full_bar[ci % stages], (uint32_t)((ci / stages) & 1))) {
+      if (!wait_warp(&full_bar[rg.s], (uint32_t)(rg.r & 1))) {
         failed = true;
         break;
       }
@@ -545,22 +565,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
         if (lane == 0) tc::mbar_arrive(&acc_full[a]);
         break;
       }
-      const TcMset& M = L.ms[it.x];
-      const int R = M.R, N = 4 * M.NS;
+      const TcMset& M = s_ms[it.x];
+      const int R = M.R, N = 4 * M.NS, nchunks = M.nchunks;
       const uint32_t idesc = tc::idesc_f16(FMT, 128, (uint32_t)N);
       const uint32_t dcol = tbase + (uint32_t)a * 256u;
-      for (int c = 0; c < M.nchunks; ++c, ++ci) {
-        const int s = (int)(ci % stages);
-        if (c > 0 && !wait_warp(&full_bar[s], (uint32_t)((ci / stages) & 1))) {
+      const uint32_t rstep = R == 2 ? 128u : 256u;  // accumulator columns of a tile
+      for (int c = 0; c < nchunks; ++c, ++ci, rg.next(stages)) {
+        const int s = rg.s;
+        if (c > 0 && !wait_warp(&full_bar[s], (uint32_t)(rg.r & 1))) {
           failed = true;
           break;
         }
         if (lane == 0) {
-          const uint32_t st = sbase + (uint32_t)s * (uint32_t)L.stage_bytes;
+          const uint32_t st = sbase + (uint32_t)s * stage_bytes;
           const uint64_t bdesc = desc_sw128(st + (uint32_t)R * kTcTileBytes);
           for (int r = 0; r < R; ++r) {
             const uint64_t adesc = desc_sw128(st + (uint32_t)r * kTcTileBytes);
-            const uint32_t d = dcol + (uint32_t)(r * (256 / R));
+            const uint32_t d = dcol + (uint32_t)r * rstep;
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk)
               mma_f16_ss(d, adesc + (uint64_t)(2 * kk), bdesc + (uint64_t)(2 * kk), idesc, (c | kk) != 0 ? 1u : 0u);
@@ -601,9 +622,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
       const int2 it = ring[k % kTcRing];
       if (it.x < 0) break;
       const int m = it.x, t = it.y;
-      const TcMset& M = L.ms[m];
+      const TcMset& M = s_ms[m];
       const int R = M.R, NS = M.NS, nch = NS >> 3;
-      const int64_t D = L.groups[M.group].D;
+      const int64_t D = s_groups[M.group].D;
       const uint32_t laneD = (uint32_t)lane * (uint32_t)D;
       // every column chunk this warp owns (at most two: R * NS <= 64) is read
       // out of tensor memory first and the accumulator slot released, so the
@@ -1000,6 +1021,11 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     tc_groups_last_ += (int)packs[li].size();
+    if (done_fn_) {
+      std::vector<int> egs;
+      for (int gi : packs[li]) egs.push_back(gmap[gi]);
+      notify_done(egs, stream);
+    }
   }
   return FDSP_OK;
 }

@@ -275,6 +275,17 @@ class PolyEngine {
   // sequence keeps its shape).  Applies on the legacy default stream, or on a
   // stream the caller is capturing, launch directly.
   void set_graph(bool on);
+  // Completion hook of the next applies: after the last launch that writes
+  // the outputs of some decimation groups, fn(ctx, channels, count, stream)
+  // runs on the host with the channels whose outputs are then enqueued
+  // complete on `stream` (the apply_host entry points start their
+  // device-to-host copies from it while later groups compute).  Applies
+  // launch directly (no graph) while a hook is set.
+  using DoneFn = void (*)(void* ctx, const int* chans, int count, cudaStream_t stream);
+  void set_done_hook(DoneFn fn, void* ctx) {
+    done_fn_ = fn;
+    done_ctx_ = ctx;
+  }
   int graph_replays() const { return graph_replays_; }
   void group_info(int g, uint32_t* D, int* Qt, int* use_tc) const {
     *D = groups_[g].D;
@@ -337,6 +348,9 @@ class PolyEngine {
   std::vector<cudaEvent_t> prof_ev_;   // autotuning: [2 g] / [2 g + 1] around group g
   std::vector<int> prof_hit_;          // group g launched in the timed apply
   bool kprof_ = false;                 // kernel timing on
+  DoneFn done_fn_ = nullptr;           // completion hook (apply_host overlap)
+  void* done_ctx_ = nullptr;
+  void notify_done(const std::vector<int>& egroups, cudaStream_t stream);
   std::vector<cudaEvent_t> kprof_ev_;  // (start, end) pairs of the timed launches
   size_t kprof_used_ = 0;
   cudaEvent_t kprof_event();           // next free event of the pool

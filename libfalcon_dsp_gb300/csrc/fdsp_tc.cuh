@@ -137,6 +137,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity, u
   return done != 0;
 }
 
+// One poll without a suspend hint: the hardware's own time limit applies
+// (for the latency-critical producer and MMA threads).
+__device__ __forceinline__ bool mbar_try_wait_nohint(uint64_t* mbar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n"
+      ".reg .pred P1;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
+      "selp.b32 %0, 1, 0, P1;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(smem_u32(mbar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Bounded wait on the latency-critical path: polls without a suspend hint,
+// gives up after 16 x max_polls polls (each returns after a hardware-chosen
+// time limit, well below the hinted 2 us).
+__device__ __forceinline__ bool mbar_wait_bounded_fast(uint64_t* mbar, uint32_t parity, uint32_t max_polls) {
+  for (uint32_t i = 0; i < max_polls; ++i)
+    for (int j = 0; j < 16; ++j)
+      if (mbar_try_wait_nohint(mbar, parity)) return true;
+  return false;
+}
+
 // Bounded wait: gives up after `max_polls` polls (each suspends at most
 // ~2 us, so 2^20 polls stay within a few seconds) and returns false.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parity, uint32_t max_polls) {

@@ -52,9 +52,9 @@ constexpr int kTcChunkTaps = 16;       // taps per K chunk: 128 bytes of A per r
 constexpr int kTcTileBytes = kTcRows * 128;
 constexpr int kTcMsetSlots = 64;       // slots per merge set (N = 4 NS <= 256)
 constexpr int kTcStageMaxBytes = 49152;
-constexpr int kTcSmemDyn = 225 * 1024; // dynamic shared memory ceiling (227 KB minus static and alignment)
+constexpr int kTcSmemDyn = 223 * 1024; // dynamic shared memory ceiling (227 KB minus static and alignment)
 constexpr int kTcMaxStages = 6;
-constexpr int kTcEpiSlotBytes = 64;    // per-slot epilogue constants staged in shared memory
+constexpr int kTcEpiSlotBytes = 48;    // per-slot epilogue constants staged in shared memory
 
 // ---- launch records (kernel parameters; shared with the device code) -----
 struct TcGroup {
