@@ -397,6 +397,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   __shared__ uint32_t tmem_base_s;
   __shared__ int2 ring[kTcRing];       // item k: (merge set, item index); merge set -1 ends the sequence
   __shared__ TcCursor cursor;
+  __shared__ int2 batch[32];           // the producer's next items (merge set, item index)
   __shared__ TcMset s_ms[kTcMaxMsets];       // merge sets and groups of the launch (read per item)
   __shared__ TcGroup s_groups[kTcMaxGroups];
   const int tid = threadIdx.x;
@@ -468,115 +469,119 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    // the whole warp walks the item sequence; lane 0 takes the waits (their
-    // outcome is shared with the warp) and issues the copies
+    // Lane 0 alone waits and issues the copies; the whole warp only refills
+    // a batch of up to 32 items with the warp-parallel cursor between them.
+    // (Keeping the other lanes in warp-synchronous calls around every wait
+    // slowed the MMA stream to less than half its rate.)
     TcCursor& cur = cursor;
     cur.init(L, s_ms, s_groups, blockIdx.x, lane);
     __syncwarp();
-    auto wait0 = [&](uint64_t* bar, uint32_t parity) {
-      bool ok = true;
-      if (lane == 0) ok = tc::mbar_wait_bounded_fast(bar, parity, poll);
-      return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-    };
-    int64_t ci = 0;  // chunks issued
-    TcRing rg;       // its stage and round
+    int64_t ci = 0;  // chunks issued (lane 0)
+    TcRing rg;       // their stage and round
     int64_t k = 0;   // items announced
     bool failed = false;
-    int m = 0, t = 0;
-    while (!hold && !failed) {
-      const bool more = cur.next(L, s_ms, lane, &m, &t);
-      // announce item k (or the end of the sequence) with its first stage
-      {
-        const int s = rg.s;
-        const int kk = rg.r;
-        if (kk > 0 && !wait0(&empty_bar[s], (uint32_t)((kk - 1) & 1))) {
-          failed = true;
-          break;
-        }
-        if (lane == 0) ring[k % kTcRing] = make_int2(more ? m : -1, more ? t : 0);
-        ++k;
-        if (!more) {
-          if (lane == 0) tc::mbar_arrive(&full_bar[s]);  // no copies: the consumers read the end marker
-          ++ci;
-          rg.next(stages);
-          break;
+    bool done = hold;
+    while (!done) {
+      int nb = 0;
+      for (; nb < 32; ++nb) {
+        int m, t;
+        if (!cur.next(L, s_ms, lane, &m, &t)) break;
+        if (lane == 0) batch[nb] = make_int2(m, t);
+      }
+      __syncwarp();
+      if (lane == 0) {
+        for (int bi = 0; bi <= nb; ++bi) {
+          const bool more = bi < nb;
+          if (!more && nb == 32) break;  // a full batch: the sequence may go on
+          // announce item k (or the end of the sequence) with its first stage
+          if (rg.r > 0 && !tc::mbar_wait_bounded_fast(&empty_bar[rg.s], (uint32_t)((rg.r - 1) & 1), poll)) {
+            failed = true;
+            break;
+          }
+          ring[k % kTcRing] = more ? batch[bi] : make_int2(-1, 0);
+          ++k;
+          if (!more) {
+            tc::mbar_arrive(&full_bar[rg.s]);  // no copies: the consumers read the end marker
+            ++ci;
+            rg.next(stages);
+            break;
+          }
+          const int m = batch[bi].x, t = batch[bi].y;
+          const TcMset& M = s_ms[m];
+          const int D = s_groups[M.group].D;
+          const CUtensorMap* map = &P.maps[M.group];
+          const int R = M.R;
+          const uint32_t bbytes = (uint32_t)(4 * M.NS * 128);
+          const uint32_t tx = (uint32_t)R * kTcTileBytes + bbytes;
+          const int32_t x0 = 4 * (M.a % D);
+          const int32_t y0 = t * R * kTcRows + M.a / D;
+          const uint8_t* bsrc = bbuf + M.b;
+          const int nchunks = M.nchunks;
+          for (int c = 0; c < nchunks; ++c, ++ci, rg.next(stages)) {
+            const int s = rg.s;
+            // (the first chunk's stage was claimed with the announcement)
+            if (c > 0 && rg.r > 0 && !tc::mbar_wait_bounded_fast(&empty_bar[s], (uint32_t)((rg.r - 1) & 1), poll)) {
+              failed = true;
+              break;
+            }
+            const uint32_t st = sbase + (uint32_t)s * stage_bytes;
+            const uint32_t fb = tc::smem_u32(&full_bar[s]);
+            mbar_expect_tx(&full_bar[s], tx);
+            for (int r = 0; r < R; ++r)
+              tma_load_2d(st + (uint32_t)r * kTcTileBytes, map, x0 + 64 * c, y0 + r * kTcRows, fb);
+            bulk_load(st + (uint32_t)R * kTcTileBytes, bsrc + (size_t)c * bbytes, bbytes, fb);
+          }
+          if (failed) break;
         }
       }
-      const TcMset& M = s_ms[m];
-      const int D = s_groups[M.group].D;
-      const CUtensorMap* map = &P.maps[M.group];
-      const int R = M.R;
-      const uint32_t bbytes = (uint32_t)(4 * M.NS * 128);
-      const uint32_t tx = (uint32_t)R * kTcTileBytes + bbytes;
-      const int32_t x0 = 4 * (M.a % D);
-      const int32_t y0 = t * R * kTcRows + M.a / D;
-      const uint8_t* bsrc = bbuf + M.b;
-      const int nchunks = M.nchunks;
-      for (int c = 0; c < nchunks; ++c, ++ci, rg.next(stages)) {
-        const int s = rg.s;
-        const int kk = rg.r;
-        // (the first chunk's stage was claimed with the announcement)
-        if (c > 0 && kk > 0 && !wait0(&empty_bar[s], (uint32_t)((kk - 1) & 1))) {
-          failed = true;
-          break;
-        }
-        if (lane == 0) {
-          const uint32_t st = sbase + (uint32_t)s * stage_bytes;
-          const uint32_t fb = tc::smem_u32(&full_bar[s]);
-          mbar_expect_tx(&full_bar[s], tx);
-          for (int r = 0; r < R; ++r)
-            tma_load_2d(st + (uint32_t)r * kTcTileBytes, map, x0 + 64 * c, y0 + r * kTcRows, fb);
-          bulk_load(st + (uint32_t)R * kTcTileBytes, bsrc + (size_t)c * bbytes, bbytes, fb);
-        }
-        __syncwarp();
-      }
+      done = __shfl_sync(0xffffffffu, (failed || nb < 32) ? 1 : 0, 0) != 0;
     }
-    // every copy issued lands before the CTA can exit
-    for (int64_t i = (ci > stages ? ci - stages : 0); i < ci; ++i)
-      if (!wait0(&full_bar[i % stages], (uint32_t)((i / stages) & 1))) failed = true;
-    if (failed && lane == 0) atomicExch(L.err, 1);
+    if (lane == 0) {
+      // every copy issued lands before the CTA can exit
+      for (int64_t i = (ci > stages ? ci - stages : 0); i < ci; ++i)
+        if (!tc::mbar_wait_bounded_fast(&full_bar[i % stages], (uint32_t)((i / stages) & 1), poll)) failed = true;
+      if (failed) atomicExch(L.err, 1);
+    }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
-    int64_t ci = 0;
-    TcRing rg;
-    int k = 0;
-    bool failed = false, issued = false;
-    // every wait is taken by lane 0 and its outcome shared with the warp
-    auto wait_warp = [&](uint64_t* bar, uint32_t parity) {
-      bool ok = true;
-      if (lane == 0) ok = tc::mbar_wait_bounded_fast(bar, parity, poll);
-      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-      tc::fence_after_sync();
-      return ok;
-    };
-    while (true) {
-      // the first stage of item k also announces it (ring entry k)
-      if (!wait_warp(&full_bar[rg.s], (uint32_t)(rg.r & 1))) {
-        failed = true;
-        break;
-      }
-      const int2 it = ring[k % kTcRing];
-      const int a = k & 1;
-      if (k >= 2 && !wait_warp(&acc_empty[a], (uint32_t)(((k >> 1) - 1) & 1))) {
-        failed = true;
-        break;
-      }
-      if (it.x < 0) {  // end of the sequence: pass it on through the accumulator slot
-        if (lane == 0) tc::mbar_arrive(&acc_full[a]);
-        break;
-      }
-      const TcMset& M = s_ms[it.x];
-      const int R = M.R, N = 4 * M.NS, nchunks = M.nchunks;
-      const uint32_t idesc = tc::idesc_f16(FMT, 128, (uint32_t)N);
-      const uint32_t dcol = tbase + (uint32_t)a * 256u;
-      const uint32_t rstep = R == 2 ? 128u : 256u;  // accumulator columns of a tile
-      for (int c = 0; c < nchunks; ++c, ++ci, rg.next(stages)) {
-        const int s = rg.s;
-        if (c > 0 && !wait_warp(&full_bar[s], (uint32_t)(rg.r & 1))) {
+    // (lane 0 alone, for the same reason)
+    if (lane == 0) {
+      int64_t ci = 0;
+      TcRing rg;
+      int k = 0;
+      bool failed = false, issued = false;
+      auto wait1 = [&](uint64_t* bar, uint32_t parity) {
+        const bool ok = tc::mbar_wait_bounded_fast(bar, parity, poll);
+        tc::fence_after_sync();
+        return ok;
+      };
+      while (true) {
+        // the first stage of item k also announces it (ring entry k)
+        if (!wait1(&full_bar[rg.s], (uint32_t)(rg.r & 1))) {
           failed = true;
           break;
         }
-        if (lane == 0) {
+        const int2 it = ring[k % kTcRing];
+        const int a = k & 1;
+        if (k >= 2 && !wait1(&acc_empty[a], (uint32_t)(((k >> 1) - 1) & 1))) {
+          failed = true;
+          break;
+        }
+        if (it.x < 0) {  // end of the sequence: pass it on through the accumulator slot
+          tc::mbar_arrive(&acc_full[a]);
+          break;
+        }
+        const TcMset& M = s_ms[it.x];
+        const int R = M.R, N = 4 * M.NS, nchunks = M.nchunks;
+        const uint32_t idesc = tc::idesc_f16(FMT, 128, (uint32_t)N);
+        const uint32_t dcol = tbase + (uint32_t)a * 256u;
+        const uint32_t rstep = R == 2 ? 128u : 256u;  // accumulator columns of a tile
+        for (int c = 0; c < nchunks; ++c, ++ci, rg.next(stages)) {
+          const int s = rg.s;
+          if (c > 0 && !wait1(&full_bar[s], (uint32_t)(rg.r & 1))) {
+            failed = true;
+            break;
+          }
           const uint32_t st = sbase + (uint32_t)s * stage_bytes;
           const uint64_t bdesc = desc_sw128(st + (uint32_t)R * kTcTileBytes);
           for (int r = 0; r < R; ++r) {
@@ -589,14 +594,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
           tc::mma_commit(&empty_bar[s]);
           issued = true;
         }
-        __syncwarp();
+        if (failed) break;
+        tc::mma_commit(&acc_full[a]);
+        ++k;
       }
-      if (failed) break;
-      if (lane == 0) tc::mma_commit(&acc_full[a]);
-      __syncwarp();
-      ++k;
-    }
-    if (lane == 0) {
       // every MMA this CTA issued completes before its TMEM is released
       if (issued) {
         tc::mma_commit(&drain_bar);
