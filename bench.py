@@ -580,9 +580,14 @@ def run_ours(args) -> None:
                    "p999_ms": round(st["p999_ms"], 4), "blocks": st["blocks"],
                    "value": round(st["out_msps"], 1), "unit": "Msamples/s",
                    "streams": args.serve_streams, "jobs_admitted": st["admitted"], "jobs_arrived": st["arrived"],
+                   "served_fraction": round(st["served_fraction"], 4),
+                   "admit_wait_p50_ms": round(st["admit_wait_p50_ms"], 3),
+                   "admit_wait_p99_ms": round(st["admit_wait_p99_ms"], 3),
                    "seconds": round(st["wall_s"], 3),
                    "note": "latency = submit to output back in pinned host memory; jobs arrive faster than one GPU "
-                           "serves them, admission is by the memory budget and the stream limit"}
+                           "serves them (served_fraction of the arrivals are admitted within the window), admission "
+                           "is by the memory budget (one device pool, no allocation per stream) and the stream "
+                           "limit; admit_wait = arrival to admission"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

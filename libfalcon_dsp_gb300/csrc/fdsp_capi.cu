@@ -855,3 +855,21 @@ int fdsp_polar_apply_host(fdsp_polar* h, const fdsp_cf32* h_in, uint64_t n_in, f
 }
 
 }  // extern "C"
+
+int fdsp::channelizer_create_pooled(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, DevPool* pool,
+                                    cudaStream_t stream, fdsp_channelizer** out) {
+  if (!out) return FDSP_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (fs == 0 || nch == 0 || !ch) return FDSP_ERR_INVALID_ARG;
+  fdsp_channelizer* h = new (std::nothrow) fdsp_channelizer();
+  if (!h) return FDSP_ERR_ALLOC;
+  h->eng.set_pool(pool);
+  int st = h->eng.init(fs, ch, nch, false, stream);
+  if (st != FDSP_OK) {
+    delete h;
+    return st;
+  }
+  h->out.resize(nch);
+  *out = h;
+  return FDSP_OK;
+}

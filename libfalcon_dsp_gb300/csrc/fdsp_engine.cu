@@ -461,12 +461,85 @@ PolyEngine::~PolyEngine() {
     if (e) cudaEventDestroy(e);
   free_tc();
   for (auto& b : batches_) {
-    if (b.d_taps) cudaFree(b.d_taps);
+    if (b.d_taps) dfree(b.d_taps);
   }
-  if (d_nco_) cudaFree(d_nco_);
+  if (d_nco_) dfree(d_nco_);
   for (auto& h : d_hist_) {
-    if (h) cudaFree(h);
+    if (h) dfree(h);
   }
+}
+
+// ---------------------------------------------------------------------------
+// device memory: the engine's own buffers come from its pool when it has one
+// ---------------------------------------------------------------------------
+cudaError_t PolyEngine::dalloc(void** p, size_t bytes) {
+  if (!pool_) return cudaMalloc(p, bytes);
+  *p = pool_->alloc(bytes);
+  return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+}
+
+void PolyEngine::dfree(void* p) {
+  if (!p) return;
+  if (pool_) pool_->release(p);
+  else cudaFree(p);
+}
+
+DevPool::~DevPool() {
+  if (base_) cudaFree(base_);
+}
+
+int DevPool::init(size_t bytes) {
+  std::lock_guard<std::mutex> lk(mu_);
+  if (base_ || bytes == 0) return FDSP_ERR_INVALID_ARG;
+  bytes &= ~(size_t)255;
+  const cudaError_t e = cudaMalloc(&base_, bytes);
+  if (e != cudaSuccess) {
+    base_ = nullptr;
+    return cuda_status(e);
+  }
+  size_ = bytes;
+  free_.clear();
+  used_.clear();
+  free_[0] = bytes;
+  return FDSP_OK;
+}
+
+void* DevPool::alloc(size_t bytes) {
+  const size_t n = (std::max<size_t>(bytes, 1) + 255) & ~(size_t)255;
+  std::lock_guard<std::mutex> lk(mu_);
+  for (auto it = free_.begin(); it != free_.end(); ++it) {
+    if (it->second < n) continue;
+    const size_t off = it->first, len = it->second;
+    free_.erase(it);
+    if (len > n) free_[off + n] = len - n;
+    used_[off] = n;
+    return base_ + off;
+  }
+  return nullptr;
+}
+
+void DevPool::release(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(mu_);
+  const size_t off = (size_t)(static_cast<char*>(p) - base_);
+  auto u = used_.find(off);
+  if (u == used_.end()) return;
+  size_t start = off, len = u->second;
+  used_.erase(u);
+  auto nx = free_.lower_bound(start);
+  if (nx != free_.end() && nx->first == start + len) {  // merge with the next free range
+    len += nx->second;
+    nx = free_.erase(nx);
+  }
+  if (nx != free_.begin()) {  // and with the previous one
+    auto pv = std::prev(nx);
+    if (pv->first + pv->second == start) {
+      start = pv->first;
+      len += pv->second;
+      free_.erase(pv);
+    }
+  }
+  free_[start] = len;
 }
 
 static int choose_qt(uint32_t D, int tmax) {
@@ -484,7 +557,7 @@ static int choose_qt(uint32_t D, int tmax) {
   return qt;
 }
 
-int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool complex_taps) {
+int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool complex_taps, cudaStream_t stream) {
   if (nch == 0 || ch == nullptr) return FDSP_ERR_INVALID_ARG;
   if (nch > (uint32_t)kMaxChannels) return FDSP_ERR_UNSUPPORTED;
   fs_ = fs;
@@ -639,7 +712,7 @@ int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool
         }
       }
     }
-    cudaError_t e = cudaMalloc(&bt.d_taps, host.size() * sizeof(float2));
+    cudaError_t e = dalloc(reinterpret_cast<void**>(&bt.d_taps), host.size() * sizeof(float2));
     if (e != cudaSuccess) return cuda_status(e);
     e = cudaMemcpy(bt.d_taps, host.data(), host.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_status(e);
@@ -647,20 +720,25 @@ int PolyEngine::init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool
 
   std::vector<NcoConst> nco(nch);
   for (uint32_t c = 0; c < nch; ++c) nco[c] = chans_[c].nco;
-  cudaError_t e = cudaMalloc(&d_nco_, nch * sizeof(NcoConst));
+  cudaError_t e = dalloc(reinterpret_cast<void**>(&d_nco_), nch * sizeof(NcoConst));
   if (e != cudaSuccess) return cuda_status(e);
   e = cudaMemcpy(d_nco_, nco.data(), nch * sizeof(NcoConst), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_status(e);
   if (H_ > 0) {
     for (auto& h : d_hist_) {
-      e = cudaMalloc(&h, (size_t)H_ * sizeof(float2));
+      e = dalloc(reinterpret_cast<void**>(&h), (size_t)H_ * sizeof(float2));
       if (e != cudaSuccess) return cuda_status(e);
-      e = cudaMemset(h, 0, (size_t)H_ * sizeof(float2));
+      e = stream ? cudaMemsetAsync(h, 0, (size_t)H_ * sizeof(float2), stream)
+                 : cudaMemset(h, 0, (size_t)H_ * sizeof(float2));
       if (e != cudaSuccess) return cuda_status(e);
     }
   }
-  e = cudaDeviceSynchronize();
-  if (e != cudaSuccess) return cuda_status(e);
+  // with a stream the engine's applies on it follow the fill; without one
+  // every later stream must see it
+  if (!stream) {
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_status(e);
+  }
   return FDSP_OK;
 }
 

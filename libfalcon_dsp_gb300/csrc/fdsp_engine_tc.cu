@@ -63,6 +63,7 @@ namespace fdsp {
 constexpr int kTcEpiWarps = 16;                       // four per TMEM lane quarter
 constexpr int kTcThreads = 64 + 32 * kTcEpiWarps;     // producer warp, MMA warp, epilogue warps
 constexpr int kTcRing = 16;                           // items announced ahead (> stages + 2)
+constexpr int kTcBatch = 16;                          // items the producer warp finds per refill
 constexpr uint32_t kTmemCols = 512;
 
 // ---------------------------------------------------------------------------
@@ -138,39 +139,40 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 }
 
 // The sequence of items (merge set, item index) a CTA runs, walked by the
-// producer alone (its arrays in shared memory: local memory would miss L1,
-// which the stages leave small) and announced to the MMA and epilogue warps
-// through a ring of (merge set, item) entries.  Items of merge set m start at
-// input sample a + t P; the next item is the earliest start.
+// producer warp and announced to the MMA and epilogue warps through a ring of
+// (merge set, item) entries.  Items of merge set m start at input sample
+// a + t P; the next item is the earliest start (ties: the lower merge set).
+// Lane l keeps merge sets l and l + 32 in registers: its next start u, its
+// item range [cur, end) and P; a butterfly reduction picks the next item.
 struct TcCursor {
-  int32_t cur[kTcMaxMsets];
-  int32_t end[kTcMaxMsets];
-  int64_t P[kTcMaxMsets];
-  // (the lanes of a warp split the merge sets)
-  __device__ void init(const TcLaunch& L, const TcMset* ms, const TcGroup* groups, int b, int lane) {
-    for (int m = lane; m < L.nmsets; m += 32) {
+  int64_t u[2], P[2];
+  int32_t cur[2], end[2];
+  __device__ void init(const TcMset* ms, const TcGroup* groups, int nmsets, int64_t Lc, int G, int b, int lane) {
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int m = lane + 32 * i;
+      cur[i] = end[i] = 0;
+      u[i] = P[i] = 0;
+      if (m >= nmsets) continue;
       const TcMset& M = ms[m];
-      P[m] = (int64_t)M.R * kTcRows * groups[M.group].D;
+      P[i] = (int64_t)M.R * kTcRows * groups[M.group].D;
       int64_t f, l;
-      tc_item_range(M.a, P[m], M.items, L.Lc, b, L.G, &f, &l);
-      cur[m] = (int32_t)f;
-      end[m] = (int32_t)l;
+      tc_item_range(M.a, P[i], M.items, Lc, b, G, &f, &l);
+      cur[i] = (int32_t)f;
+      end[i] = (int32_t)l;
+      u[i] = (int64_t)M.a + f * P[i];
     }
   }
-  // The next item in input order (ties: the lower merge set), found by the
-  // whole warp: each lane scans every 32nd merge set, then a butterfly
-  // reduction; every lane returns the same item.
-  __device__ bool next(const TcLaunch& L, const TcMset* ms, int lane, int* m_out, int* t_out) {
+  // (whole warp; every lane returns the same item)
+  __device__ __forceinline__ bool next(int lane, int* m_out, int* t_out) {
     int64_t bu = INT64_MAX;
     int bm = INT32_MAX;
-    for (int m = lane; m < L.nmsets; m += 32) {
-      if (cur[m] >= end[m]) continue;
-      const int64_t u = (int64_t)ms[m].a + (int64_t)cur[m] * P[m];
-      if (u < bu) {
-        bu = u;
-        bm = m;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+      if (cur[i] < end[i] && u[i] < bu) {
+        bu = u[i];
+        bm = lane + 32 * i;
       }
-    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const int64_t u2 = __shfl_xor_sync(0xffffffffu, bu, o);
@@ -181,11 +183,20 @@ struct TcCursor {
       }
     }
     if (bm == INT32_MAX) return false;
+    int t = 0;
+    if ((bm & 31) == lane) {
+      const int i = bm >> 5;
+      t = i ? cur[1] : cur[0];
+      if (i) {
+        cur[1]++;
+        u[1] += P[1];
+      } else {
+        cur[0]++;
+        u[0] += P[0];
+      }
+    }
     *m_out = bm;
-    *t_out = cur[bm];
-    __syncwarp();
-    if (lane == 0) cur[bm]++;
-    __syncwarp();
+    *t_out = __shfl_sync(0xffffffffu, t, bm & 31);
     return true;
   }
 };
@@ -396,8 +407,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   __shared__ __align__(8) uint64_t drain_bar;
   __shared__ uint32_t tmem_base_s;
   __shared__ int2 ring[kTcRing];       // item k: (merge set, item index); merge set -1 ends the sequence
-  __shared__ TcCursor cursor;
-  __shared__ int2 batch[32];           // the producer's next items (merge set, item index)
+  __shared__ int2 batch[kTcBatch];     // the producer's next items (merge set, item index)
   __shared__ TcMset s_ms[kTcMaxMsets];       // merge sets and groups of the launch (read per item)
   __shared__ TcGroup s_groups[kTcMaxGroups];
   const int tid = threadIdx.x;
@@ -470,12 +480,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     // Lane 0 alone waits and issues the copies; the whole warp only refills
-    // a batch of up to 32 items with the warp-parallel cursor between them.
+    // a batch of up to kTcBatch items with the warp-parallel cursor between
+    // them.
     // (Keeping the other lanes in warp-synchronous calls around every wait
     // slowed the MMA stream to less than half its rate.)
-    TcCursor& cur = cursor;
-    cur.init(L, s_ms, s_groups, blockIdx.x, lane);
-    __syncwarp();
+    TcCursor cur;
+    cur.init(s_ms, s_groups, L.nmsets, L.Lc, L.G, blockIdx.x, lane);
     int64_t ci = 0;  // chunks issued (lane 0)
     TcRing rg;       // their stage and round
     int64_t k = 0;   // items announced
@@ -483,16 +493,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
     bool done = hold;
     while (!done) {
       int nb = 0;
-      for (; nb < 32; ++nb) {
+      for (; nb < kTcBatch; ++nb) {
         int m, t;
-        if (!cur.next(L, s_ms, lane, &m, &t)) break;
+        if (!cur.next(lane, &m, &t)) break;
         if (lane == 0) batch[nb] = make_int2(m, t);
       }
       __syncwarp();
       if (lane == 0) {
         for (int bi = 0; bi <= nb; ++bi) {
           const bool more = bi < nb;
-          if (!more && nb == 32) break;  // a full batch: the sequence may go on
+          if (!more && nb == kTcBatch) break;  // a full batch: the sequence may go on
           // announce item k (or the end of the sequence) with its first stage
           if (rg.r > 0 && !tc::mbar_wait_bounded_fast(&empty_bar[rg.s], (uint32_t)((rg.r - 1) & 1), poll)) {
             failed = true;
@@ -534,7 +544,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
           if (failed) break;
         }
       }
-      done = __shfl_sync(0xffffffffu, (failed || nb < 32) ? 1 : 0, 0) != 0;
+      done = __shfl_sync(0xffffffffu, (failed || nb < kTcBatch) ? 1 : 0, 0) != 0;
     }
     if (lane == 0) {
       // every copy issued lands before the CTA can exit
@@ -738,11 +748,11 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 void PolyEngine::free_tc() {
-  if (d_ctaps_) cudaFree(d_ctaps_);
-  if (d_ctab_) cudaFree(d_ctab_);
-  if (d_xhl_) cudaFree(d_xhl_);
-  if (d_bbuf_) cudaFree(d_bbuf_);
-  if (d_tcrec_) cudaFree(d_tcrec_);
+  if (d_ctaps_) dfree(d_ctaps_);
+  if (d_ctab_) dfree(d_ctab_);
+  if (d_xhl_) dfree(d_xhl_);
+  if (d_bbuf_) dfree(d_bbuf_);
+  if (d_tcrec_) dfree(d_tcrec_);
   if (h_err_) cudaFreeHost(h_err_);
   d_ctaps_ = nullptr;
   d_ctab_ = nullptr;
@@ -791,13 +801,13 @@ int PolyEngine::build_tc(int fmt) {
       }
     }
   }
-  cudaError_t err = cudaMalloc(&d_ctaps_, total * sizeof(float2));
+  cudaError_t err = dalloc(reinterpret_cast<void**>(&d_ctaps_), total * sizeof(float2));
   if (err == cudaSuccess) err = cudaMemcpy(d_ctaps_, g.data(), total * sizeof(float2), cudaMemcpyHostToDevice);
   std::vector<const float2*> tab(chans_.size());
   for (size_t c = 0; c < chans_.size(); ++c) tab[c] = d_ctaps_ + off[c];
-  if (err == cudaSuccess) err = cudaMalloc(&d_ctab_, tab.size() * sizeof(float2*));
+  if (err == cudaSuccess) err = dalloc(reinterpret_cast<void**>(&d_ctab_), tab.size() * sizeof(float2*));
   if (err == cudaSuccess) err = cudaMemcpy(d_ctab_, tab.data(), tab.size() * sizeof(float2*), cudaMemcpyHostToDevice);
-  if (err == cudaSuccess) err = cudaMalloc(&d_tcrec_, sizeof(TcLaunch));
+  if (err == cudaSuccess) err = dalloc(reinterpret_cast<void**>(&d_tcrec_), sizeof(TcLaunch));
   if (err == cudaSuccess) err = cudaHostAlloc(&h_err_, sizeof(int), cudaHostAllocMapped);
   if (err == cudaSuccess) {
     *h_err_ = 0;
@@ -908,17 +918,17 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     b_need = std::max(b_need, p.b_bytes);
   }
   if ((size_t)xhl_need > xhl_cap_) {
-    if (d_xhl_) cudaFree(d_xhl_);
+    if (d_xhl_) dfree(d_xhl_);
     d_xhl_ = nullptr;
     xhl_cap_ = 0;
-    FDSP_TRY(cuda_status(cudaMalloc(&d_xhl_, (size_t)xhl_need * sizeof(uint2))));
+    FDSP_TRY(cuda_status(dalloc(reinterpret_cast<void**>(&d_xhl_), (size_t)xhl_need * sizeof(uint2))));
     xhl_cap_ = (size_t)xhl_need;
   }
   if (b_need > bbuf_cap_) {
-    if (d_bbuf_) cudaFree(d_bbuf_);
+    if (d_bbuf_) dfree(d_bbuf_);
     d_bbuf_ = nullptr;
     bbuf_cap_ = 0;
-    FDSP_TRY(cuda_status(cudaMalloc(&d_bbuf_, b_need)));
+    FDSP_TRY(cuda_status(dalloc(reinterpret_cast<void**>(&d_bbuf_), b_need)));
     bbuf_cap_ = b_need;
   }
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();

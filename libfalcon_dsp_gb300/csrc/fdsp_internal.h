@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "fdsp_c.h"
@@ -182,6 +183,32 @@ struct EngineChannel {
   NcoConst nco;
 };
 
+// Device memory pool: one cudaMalloc'd region handed out first-fit (256-byte
+// aligned, neighbours coalesced on release; host-side bookkeeping under a
+// mutex).  The stream server gives it to its channelizers so that opening,
+// closing and resetting streams allocate nothing from the driver.
+class DevPool {
+ public:
+  ~DevPool();
+  int init(size_t bytes);            // the one cudaMalloc
+  void* alloc(size_t bytes);         // nullptr when no free range fits
+  void release(void* p);
+  size_t size() const { return size_; }
+
+ private:
+  char* base_ = nullptr;
+  size_t size_ = 0;
+  std::map<size_t, size_t> free_;    // offset -> bytes
+  std::map<size_t, size_t> used_;    // offset -> bytes
+  std::mutex mu_;
+};
+
+// A channelizer whose device memory comes from `pool` and whose initial
+// history fill is enqueued on `stream` (no allocation from the driver and no
+// device synchronisation: the stream server's open path).
+int channelizer_create_pooled(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, DevPool* pool,
+                              cudaStream_t stream, fdsp_channelizer** out);
+
 struct EngineClass {   // channels with identical (up, down) share streaming state
   uint32_t up, down;
   uint32_t phase;      // reference coeff_phase
@@ -216,7 +243,13 @@ class PolyEngine {
   // complex_taps: FIR semantics (taps used as complex numbers);
   // otherwise resampler semantics (only the real part of each tap is used,
   // falcon_dsp_polyphase_resampler.cc:286-299).
-  int init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool complex_taps);
+  // stream: where the initial history fill is enqueued (the engine's applies
+  // on that stream follow it); nullptr: filled and synchronised on the device
+  int init(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nch, bool complex_taps, cudaStream_t stream = nullptr);
+  // device memory of later allocations from `pool` (set before init)
+  void set_pool(DevPool* pool) { pool_ = pool; }
+  cudaError_t dalloc(void** p, size_t bytes);
+  void dfree(void* p);
   ~PolyEngine();
 
   int out_counts(uint64_t n_in, uint64_t* n_out) const;
@@ -349,6 +382,7 @@ class PolyEngine {
   std::vector<int> prof_hit_;          // group g launched in the timed apply
   bool kprof_ = false;                 // kernel timing on
   DoneFn done_fn_ = nullptr;           // completion hook (apply_host overlap)
+  DevPool* pool_ = nullptr;            // device memory source (nullptr: cudaMalloc)
   void* done_ctx_ = nullptr;
   void notify_done(const std::vector<int>& egroups, cudaStream_t stream);
   std::vector<cudaEvent_t> kprof_ev_;  // (start, end) pairs of the timed launches

@@ -10,6 +10,13 @@
 // device footprint fits the server's memory budget and the active-stream
 // limit, so new work starts as soon as earlier streams close.
 //
+// Device memory: the server takes its budget as one pool when it is created
+// (csrc/fdsp_engine.cu DevPool); every stream's channelizer (taps, NCO
+// constants, history), input buffer and output arena come from it, and the
+// CUDA streams of closed streams are kept for the next ones, so opening and
+// closing streams call neither cudaMalloc/cudaFree nor a device-wide
+// synchronisation (only the closing stream is synchronised).
+//
 // The reference has no server; its channelizer classes are one blocking
 // apply() per object (hdr/transform/falcon_dsp_multi_rate_channelizer_cuda.h:113).
 #include <algorithm>
@@ -72,12 +79,13 @@ void CUDART_CB on_block_done(void* p) {
   t->q->cv.notify_one();
 }
 
-void free_stream(ServeStream& s) {
+// Returns the stream's memory to the pool and its CUDA stream to `spare`.
+void free_stream(ServeStream& s, fdsp::DevPool& pool, std::vector<cudaStream_t>& spare) {
   if (s.cs) cudaStreamSynchronize(s.cs);
   if (s.ch) fdsp_channelizer_destroy(s.ch);
-  if (s.d_in) cudaFree(s.d_in);
-  if (s.d_arena) cudaFree(s.d_arena);
-  if (s.cs) cudaStreamDestroy(s.cs);
+  pool.release(s.d_in);
+  pool.release(s.d_arena);
+  if (s.cs) spare.push_back(s.cs);
   s = ServeStream();
 }
 
@@ -94,6 +102,11 @@ struct fdsp_server {
   uint64_t outputs = 0;
   std::mutex mu;
   DoneQueue done;
+  fdsp::DevPool pool;                   // the budget's device memory
+  std::vector<cudaStream_t> spare;      // CUDA streams of closed streams
+  ~fdsp_server() {
+    for (cudaStream_t c : spare) cudaStreamDestroy(c);
+  }
 };
 
 using namespace fdsp;
@@ -119,13 +132,28 @@ extern "C" int fdsp_server_create(uint64_t budget_bytes, uint32_t max_active, fd
   if (!s) return FDSP_ERR_ALLOC;
   s->budget = budget_bytes;
   s->max_active = max_active;
+  // the pool: the budget, or what the device has free less 1 GiB
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+    delete s;
+    return FDSP_ERR_CUDA;
+  }
+  const size_t reserve = (size_t)1 << 30;
+  const size_t pool_b = std::min<uint64_t>(budget_bytes, free_b > reserve ? free_b - reserve : free_b / 2);
+  const int rc = s->pool.init(pool_b);
+  if (rc != FDSP_OK) {
+    delete s;
+    return rc;
+  }
+  s->budget = std::min<uint64_t>(budget_bytes, s->pool.size());
   *out = s;
   return FDSP_OK;
 }
 
 extern "C" int fdsp_server_destroy(fdsp_server* s) {
   if (!s) return FDSP_ERR_NOT_INITIALIZED;
-  for (auto& kv : s->streams) free_stream(kv.second);
+  for (auto& kv : s->streams) free_stream(kv.second, s->pool, s->spare);
+  s->streams.clear();
   delete s;
   return FDSP_OK;
 }
@@ -144,10 +172,21 @@ extern "C" int fdsp_server_open(fdsp_server* s, uint32_t fs, const fdsp_channel_
   st.max_block = max_block;
   st.footprint = fp;
   st.nch = nch;
-  int rc = fdsp_channelizer_create(fs, ch, nch, &st.ch);
+  int rc = FDSP_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->spare.empty()) {
+      st.cs = s->spare.back();
+      s->spare.pop_back();
+    }
+  }
+  if (!st.cs) rc = cuda_status(cudaStreamCreateWithFlags(&st.cs, cudaStreamNonBlocking));
+  if (rc == FDSP_OK) rc = fdsp::channelizer_create_pooled(fs, ch, nch, &s->pool, st.cs, &st.ch);
   if (rc == FDSP_OK && precision != FDSP_PRECISION_FP32) rc = fdsp_channelizer_set_precision(st.ch, precision);
-  if (rc == FDSP_OK) rc = cuda_status(cudaStreamCreateWithFlags(&st.cs, cudaStreamNonBlocking));
-  if (rc == FDSP_OK) rc = cuda_status(cudaMalloc(&st.d_in, 8 * max_block));
+  if (rc == FDSP_OK) {
+    st.d_in = static_cast<float2*>(s->pool.alloc(8 * max_block));
+    if (!st.d_in) rc = FDSP_ERR_CAPACITY;
+  }
   st.d_out.assign(nch, nullptr);
   st.cap.assign(nch, 0);
   uint64_t total = 0;
@@ -155,11 +194,14 @@ extern "C" int fdsp_server_open(fdsp_server* s, uint32_t fs, const fdsp_channel_
     st.cap[c] = (max_block * ch[c].up_rate + ch[c].down_rate - 1) / ch[c].down_rate + 2;
     total += st.cap[c];
   }
-  if (rc == FDSP_OK) rc = cuda_status(cudaMalloc(&st.d_arena, 8 * total));
+  if (rc == FDSP_OK) {
+    st.d_arena = static_cast<float2*>(s->pool.alloc(8 * total));
+    if (!st.d_arena) rc = FDSP_ERR_CAPACITY;
+  }
   for (uint32_t c = 0, off = 0; c < nch && rc == FDSP_OK; off += (uint32_t)st.cap[c], ++c) st.d_out[c] = st.d_arena + off;
   std::lock_guard<std::mutex> lk(s->mu);
   if (rc != FDSP_OK) {
-    free_stream(st);
+    free_stream(st, s->pool, s->spare);
     s->used -= fp;
     return rc;
   }
@@ -256,7 +298,7 @@ extern "C" int fdsp_server_close(fdsp_server* s, uint32_t sid) {
   auto it = s->streams.find(sid);
   if (it == s->streams.end()) return FDSP_ERR_INVALID_ARG;
   s->used -= it->second.footprint;
-  free_stream(it->second);  // waits for the stream's blocks
+  free_stream(it->second, s->pool, s->spare);  // waits for the stream's blocks
   s->streams.erase(it);
   return FDSP_OK;
 }

@@ -233,5 +233,7 @@ def run_serving(duration_s: float = 5.0, rate_hz: float = 2000.0, seed: int = 4,
     st = srv.stats()
     st.update(wall_s=wall, arrived=arrived, admitted=admitted, completed_jobs=completed_jobs,
               out_msps=st["outputs"] / wall / 1e6,
-              admit_wait_p50_ms=1e3 * float(np.median(wait_admit)) if wait_admit else 0.0)
+              admit_wait_p50_ms=1e3 * float(np.percentile(wait_admit, 50)) if wait_admit else 0.0,
+              admit_wait_p99_ms=1e3 * float(np.percentile(wait_admit, 99)) if wait_admit else 0.0,
+              served_fraction=admitted / arrived if arrived else 0.0)
     return st
