@@ -21,10 +21,10 @@
 //      filter bank: keeping that rare path out of the filter-bank kernel
 //      roughly halved its MMA issue time.
 //
-// Per CTA (one per SM, 576 threads):
-//   warp 0      producer: walks the CTA's item sequence (shared-memory
-//               cursor) and announces each item in a ring with its first
-//               stage; per item (R tiles of one merge set) and K chunk,
+// Per CTA (one per SM, 608 threads):
+//   warp 0      producer: takes the CTA's items from the scheduler's queue
+//               and announces each in a ring with its first stage; per
+//               item (R tiles of one merge set) and K chunk,
 //               waits for a free stage, then R TMA tile loads of A and one
 //               bulk copy of the B chunk, completing on the stage barrier;
 //   warp 1      MMA issuer: per chunk 4 MMAs (K = 16) per tile into the
@@ -32,7 +32,10 @@
 //               chunk's commit hands the slot to the epilogue;
 //   warps 2-17  epilogue: four warps per TMEM lane quarter; each reads its
 //               (at most two) 8-slot column chunks out of tensor memory,
-//               releases the slot, then rotates and stores.
+//               releases the slot, then rotates and stores;
+//   warp 18     scheduler: finds the CTA's next items (a warp-parallel
+//               cursor over the merge sets) and queues them for warp 0.
+// Warps 0 and 1 run their loops in lane 0 alone.
 // Two accumulator slots of 256 columns (R tiles x N columns each) let the
 // MMAs of one item run while the epilogue drains the previous one.
 //
@@ -61,9 +64,10 @@
 namespace fdsp {
 
 constexpr int kTcEpiWarps = 16;                       // four per TMEM lane quarter
-constexpr int kTcThreads = 64 + 32 * kTcEpiWarps;     // producer warp, MMA warp, epilogue warps
+constexpr int kTcSchedWarp = 2 + kTcEpiWarps;         // the item scheduler (after the epilogue warps)
+constexpr int kTcThreads = 96 + 32 * kTcEpiWarps;     // producer, MMA, epilogue and scheduler warps
 constexpr int kTcRing = 16;                           // items announced ahead (> stages + 2)
-constexpr int kTcBatch = 16;                          // items the producer warp finds per refill
+constexpr int kTcQueue = 64;                          // items the scheduler warp finds ahead
 constexpr uint32_t kTmemCols = 512;
 
 // ---------------------------------------------------------------------------
@@ -407,7 +411,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   __shared__ __align__(8) uint64_t drain_bar;
   __shared__ uint32_t tmem_base_s;
   __shared__ int2 ring[kTcRing];       // item k: (merge set, item index); merge set -1 ends the sequence
-  __shared__ int2 batch[kTcBatch];     // the producer's next items (merge set, item index)
+  __shared__ int2 q_items[kTcQueue];   // scheduler -> producer: item i at i % kTcQueue
+  __shared__ int q_prod, q_cons;       // items written / taken
   __shared__ TcMset s_ms[kTcMaxMsets];       // merge sets and groups of the launch (read per item)
   __shared__ TcGroup s_groups[kTcMaxGroups];
   const int tid = threadIdx.x;
@@ -426,6 +431,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
     tc::tmem_alloc(&tmem_base_s, kTmemCols);
     tc::tmem_relinquish();
   }
+  if (tid == 0) q_prod = q_cons = 0;
   if (tid == 32) {
     for (int i = 0; i < stages; ++i) {
       tc::mbar_init(&full_bar[i], 1);
@@ -479,79 +485,106 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    // Lane 0 alone waits and issues the copies; the whole warp only refills
-    // a batch of up to kTcBatch items with the warp-parallel cursor between
-    // them.
-    // (Keeping the other lanes in warp-synchronous calls around every wait
-    // slowed the MMA stream to less than half its rate.)
-    TcCursor cur;
-    cur.init(s_ms, s_groups, L.nmsets, L.Lc, L.G, blockIdx.x, lane);
-    int64_t ci = 0;  // chunks issued (lane 0)
-    TcRing rg;       // their stage and round
-    int64_t k = 0;   // items announced
-    bool failed = false;
-    bool done = hold;
-    while (!done) {
-      int nb = 0;
-      for (; nb < kTcBatch; ++nb) {
-        int m, t;
-        if (!cur.next(lane, &m, &t)) break;
-        if (lane == 0) batch[nb] = make_int2(m, t);
-      }
-      __syncwarp();
-      if (lane == 0) {
-        for (int bi = 0; bi <= nb; ++bi) {
-          const bool more = bi < nb;
-          if (!more && nb == kTcBatch) break;  // a full batch: the sequence may go on
-          // announce item k (or the end of the sequence) with its first stage
-          if (rg.r > 0 && !tc::mbar_wait_bounded_fast(&empty_bar[rg.s], (uint32_t)((rg.r - 1) & 1), poll)) {
+    // Lane 0 alone waits and issues the copies (keeping the other lanes in
+    // warp-synchronous calls around every wait slowed the MMA stream to less
+    // than half its rate); its items come from the scheduler warp's queue.
+    if (lane == 0) {
+      int64_t ci = 0;  // chunks issued
+      TcRing rg;       // their stage and round
+      int64_t k = 0;   // items announced
+      bool failed = false;
+      while (!hold && !failed) {
+        // item k from the scheduler (bounded wait)
+        uint32_t polls = 0;
+        while (*reinterpret_cast<volatile int*>(&q_prod) <= k) {
+          if (++polls > poll) {
             failed = true;
             break;
           }
-          ring[k % kTcRing] = more ? batch[bi] : make_int2(-1, 0);
-          ++k;
-          if (!more) {
-            tc::mbar_arrive(&full_bar[rg.s]);  // no copies: the consumers read the end marker
-            ++ci;
-            rg.next(stages);
+          __nanosleep(32);
+        }
+        if (failed) break;
+        __threadfence_block();  // the item was written before the count
+        const volatile int* qi = reinterpret_cast<volatile int*>(&q_items[k % kTcQueue]);
+        const int2 item = make_int2(qi[0], qi[1]);
+        __threadfence_block();
+        *reinterpret_cast<volatile int*>(&q_cons) = (int)(k + 1);
+        const bool more = item.x >= 0;
+        // announce item k (or the end of the sequence) with its first stage
+        if (rg.r > 0 && !tc::mbar_wait_bounded_fast(&empty_bar[rg.s], (uint32_t)((rg.r - 1) & 1), poll)) {
+          failed = true;
+          break;
+        }
+        ring[k % kTcRing] = item;
+        ++k;
+        if (!more) {
+          tc::mbar_arrive(&full_bar[rg.s]);  // no copies: the consumers read the end marker
+          ++ci;
+          rg.next(stages);
+          break;
+        }
+        const int m = item.x, t = item.y;
+        const TcMset& M = s_ms[m];
+        const int D = s_groups[M.group].D;
+        const CUtensorMap* map = &P.maps[M.group];
+        const int R = M.R;
+        const uint32_t bbytes = (uint32_t)(4 * M.NS * 128);
+        const uint32_t tx = (uint32_t)R * kTcTileBytes + bbytes;
+        const int32_t x0 = 4 * (M.a % D);
+        const int32_t y0 = t * R * kTcRows + M.a / D;
+        const uint8_t* bsrc = bbuf + M.b;
+        const int nchunks = M.nchunks;
+        for (int c = 0; c < nchunks; ++c, ++ci, rg.next(stages)) {
+          const int s = rg.s;
+          // (the first chunk's stage was claimed with the announcement)
+          if (c > 0 && rg.r > 0 && !tc::mbar_wait_bounded_fast(&empty_bar[s], (uint32_t)((rg.r - 1) & 1), poll)) {
+            failed = true;
             break;
           }
-          const int m = batch[bi].x, t = batch[bi].y;
-          const TcMset& M = s_ms[m];
-          const int D = s_groups[M.group].D;
-          const CUtensorMap* map = &P.maps[M.group];
-          const int R = M.R;
-          const uint32_t bbytes = (uint32_t)(4 * M.NS * 128);
-          const uint32_t tx = (uint32_t)R * kTcTileBytes + bbytes;
-          const int32_t x0 = 4 * (M.a % D);
-          const int32_t y0 = t * R * kTcRows + M.a / D;
-          const uint8_t* bsrc = bbuf + M.b;
-          const int nchunks = M.nchunks;
-          for (int c = 0; c < nchunks; ++c, ++ci, rg.next(stages)) {
-            const int s = rg.s;
-            // (the first chunk's stage was claimed with the announcement)
-            if (c > 0 && rg.r > 0 && !tc::mbar_wait_bounded_fast(&empty_bar[s], (uint32_t)((rg.r - 1) & 1), poll)) {
-              failed = true;
-              break;
-            }
-            const uint32_t st = sbase + (uint32_t)s * stage_bytes;
-            const uint32_t fb = tc::smem_u32(&full_bar[s]);
-            mbar_expect_tx(&full_bar[s], tx);
-            for (int r = 0; r < R; ++r)
-              tma_load_2d(st + (uint32_t)r * kTcTileBytes, map, x0 + 64 * c, y0 + r * kTcRows, fb);
-            bulk_load(st + (uint32_t)R * kTcTileBytes, bsrc + (size_t)c * bbytes, bbytes, fb);
-          }
-          if (failed) break;
+          const uint32_t st = sbase + (uint32_t)s * stage_bytes;
+          const uint32_t fb = tc::smem_u32(&full_bar[s]);
+          mbar_expect_tx(&full_bar[s], tx);
+          for (int r = 0; r < R; ++r)
+            tma_load_2d(st + (uint32_t)r * kTcTileBytes, map, x0 + 64 * c, y0 + r * kTcRows, fb);
+          bulk_load(st + (uint32_t)R * kTcTileBytes, bsrc + (size_t)c * bbytes, bbytes, fb);
         }
       }
-      done = __shfl_sync(0xffffffffu, (failed || nb < kTcBatch) ? 1 : 0, 0) != 0;
-    }
-    if (lane == 0) {
       // every copy issued lands before the CTA can exit
       for (int64_t i = (ci > stages ? ci - stages : 0); i < ci; ++i)
         if (!tc::mbar_wait_bounded_fast(&full_bar[i % stages], (uint32_t)((i / stages) & 1), poll)) failed = true;
       if (failed) atomicExch(L.err, 1);
     }
+  } else if (warp == kTcSchedWarp) {
+    // ------------------------------------------------------------ scheduler
+    // The CTA's item sequence (warp-parallel cursor), kTcQueue items ahead of
+    // the producer; an item with merge set -1 ends it.
+    TcCursor cur;
+    cur.init(s_ms, s_groups, L.nmsets, L.Lc, L.G, blockIdx.x, lane);
+    bool failed = false;
+    for (int i = 0; !hold; ++i) {
+      int m = -1, t = 0;
+      const bool more = cur.next(lane, &m, &t);
+      if (lane == 0) {
+        uint32_t polls = 0;
+        while (i - *reinterpret_cast<volatile int*>(&q_cons) >= kTcQueue) {  // room in the queue
+          if (++polls > poll) {
+            failed = true;
+            break;
+          }
+          __nanosleep(64);
+        }
+        if (!failed) {
+          volatile int* qi = reinterpret_cast<volatile int*>(&q_items[i % kTcQueue]);
+          qi[0] = more ? m : -1;
+          qi[1] = more ? t : 0;
+          __threadfence_block();
+          *reinterpret_cast<volatile int*>(&q_prod) = i + 1;
+        }
+      }
+      failed = __shfl_sync(0xffffffffu, failed ? 1 : 0, 0) != 0;
+      if (!more || failed) break;
+    }
+    if (failed && lane == 0) atomicExch(L.err, 1);
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     // (lane 0 alone, for the same reason)
