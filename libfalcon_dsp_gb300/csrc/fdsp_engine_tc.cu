@@ -52,6 +52,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstdint>
 #include <cmath>
 #include <cstring>
@@ -309,6 +310,9 @@ struct TcEpiSlot {
   uint32_t pair;  // 1: the next slot holds this channel's next output (one 16-byte store)
 };
 static_assert(sizeof(TcEpiSlot) == kTcEpiSlotBytes, "epilogue slot table layout");
+static_assert(offsetof(TcEpiSlot, om) == 8 && offsetof(TcEpiSlot, R) == 32 && offsetof(TcEpiSlot, J) == 36 &&
+                  offsetof(TcEpiSlot, U) == 40 && offsetof(TcEpiSlot, Tm1) == 42 && offsetof(TcEpiSlot, pair) == 44,
+              "the epilogue reads a slot record as two 16-byte halves");
 
 // Outputs whose window crosses the NCO rollover (or whose counter leaves the
 // fast path's 32-bit range) were stored unrotated; rotate_prep/rotate_apply
@@ -395,6 +399,13 @@ __global__ void __launch_bounds__(128) tc_fix_kernel(const __grid_constant__ TcL
     if (j1 > J - 1) j1 = J - 1;
     for (int64_t j = j0; j <= j1; ++j) tc_fix_exact(L, s, j, Dp, out + (uint64_t)S.U * (uint64_t)j);
   }
+}
+
+// 16-byte shared-memory load (one instruction for four fields of a slot record).
+__device__ __forceinline__ uint4 lds128(uint32_t addr) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];\n" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(addr));
+  return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -717,36 +728,45 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
                        : (uint32_t)__umul64hi(E.fm * (uint64_t)(uint32_t)v, (uint64_t)E.R);
           }
         }
-        float2 o[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          const TcEpiSlot& E = E8[e];
-          const uint32_t P0 = __shfl_sync(0xffffffffu, p0, e);
-          const float2 y0 = make_float2(ya[2 * e], ya[2 * e + 1]);
-          uint32_t pc = P0 + laneD;
-          pc = pc >= E.R ? pc - E.R : pc;
-          const bool fast = pc + E.Tm1 < E.R || E.om == 0;
-          const uint32_t om_lo = (uint32_t)E.om, om_hi = (uint32_t)(E.om >> 32);
-          const uint32_t turns = __umulhi(pc, om_lo) + pc * om_hi;  // bits 32..63 of pc * om: 2^-32 turns
-          float sn, cs;
-          __sincosf((float)(int32_t)turns * 1.4629180792671596e-09f, &sn, &cs);  // 2 pi / 2^32
-          const float2 y = cmul_nco(y0, make_float2(cs, sn));
-          o[e] = fast ? y : y0;  // windows across the NCO rollover: unrotated, for tc_fix_kernel
-        }
-        // stores: a slot and the next one holding the same channel's next
-        // output go out as one 16-byte store (contiguous across the lanes
-        // when the channel's outputs interleave by two)
+        // per pair of slots: their constants as two 16-byte shared loads each
+        // ({out, om} and {R, J, U | Tm1 << 16, pair}), the rotation, and one
+        // 16-byte store where a slot and the next hold the same channel's
+        // consecutive outputs (contiguous across the lanes when the outputs
+        // interleave by two)
+        const uint32_t e8 = tc::smem_u32(E8);
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
-          const TcEpiSlot& E0 = E8[e];
-          const TcEpiSlot& E1 = E8[e + 1];
-          float2* d0 = reinterpret_cast<float2*>(E0.out) + (uint64_t)E0.U * (uint64_t)j;
-          const bool v0 = j < E0.J, v1 = j < E1.J;
-          if (E0.pair && v0 && v1 && (reinterpret_cast<uintptr_t>(d0) & 15u) == 0) {
-            __stcs(reinterpret_cast<float4*>(d0), make_float4(o[e].x, o[e].y, o[e + 1].x, o[e + 1].y));
+          const uint4 a0 = lds128(e8 + (uint32_t)e * kTcEpiSlotBytes);
+          const uint4 b0 = lds128(e8 + (uint32_t)e * kTcEpiSlotBytes + 32u);
+          const uint4 a1 = lds128(e8 + (uint32_t)(e + 1) * kTcEpiSlotBytes);
+          const uint4 b1 = lds128(e8 + (uint32_t)(e + 1) * kTcEpiSlotBytes + 32u);
+          float2 o[2];
+#pragma unroll
+          for (int k2 = 0; k2 < 2; ++k2) {
+            const uint4 A = k2 ? a1 : a0, Bv = k2 ? b1 : b0;
+            const uint32_t Rr = Bv.x, Tm1 = Bv.z >> 16, om_lo = A.z, om_hi = A.w;
+            const uint32_t P0 = __shfl_sync(0xffffffffu, p0, e + k2);
+            const float2 y0 = make_float2(ya[2 * (e + k2)], ya[2 * (e + k2) + 1]);
+            uint32_t pc = P0 + laneD;
+            pc = pc >= Rr ? pc - Rr : pc;
+            const bool fast = pc + Tm1 < Rr || (om_lo | om_hi) == 0u;
+            const uint32_t turns = __umulhi(pc, om_lo) + pc * om_hi;  // bits 32..63 of pc * om: 2^-32 turns
+            float sn, cs;
+            __sincosf((float)(int32_t)turns * 1.4629180792671596e-09f, &sn, &cs);  // 2 pi / 2^32
+            const float2 y = cmul_nco(y0, make_float2(cs, sn));
+            o[k2] = fast ? y : y0;  // windows across the NCO rollover: unrotated, for tc_fix_kernel
+          }
+          float2* d0 = reinterpret_cast<float2*>((uint64_t)a0.x | ((uint64_t)a0.y << 32)) +
+                       (uint64_t)(b0.z & 0xFFFFu) * (uint64_t)j;
+          const bool v0 = j < (int64_t)(int32_t)b0.y, v1 = j < (int64_t)(int32_t)b1.y;
+          if (b0.w != 0u && v0 && v1 && (reinterpret_cast<uintptr_t>(d0) & 15u) == 0) {
+            __stcs(reinterpret_cast<float4*>(d0), make_float4(o[0].x, o[0].y, o[1].x, o[1].y));
           } else {
-            if (v0) __stcs(d0, o[e]);
-            if (v1) __stcs(reinterpret_cast<float2*>(E1.out) + (uint64_t)E1.U * (uint64_t)j, o[e + 1]);
+            if (v0) __stcs(d0, o[0]);
+            if (v1)
+              __stcs(reinterpret_cast<float2*>((uint64_t)a1.x | ((uint64_t)a1.y << 32)) +
+                         (uint64_t)(b1.z & 0xFFFFu) * (uint64_t)j,
+                     o[1]);
           }
         }
       }
