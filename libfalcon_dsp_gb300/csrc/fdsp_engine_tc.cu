@@ -806,6 +806,10 @@ void PolyEngine::free_tc() {
   if (d_xhl_) dfree(d_xhl_);
   if (d_bbuf_) dfree(d_bbuf_);
   if (d_tcrec_) dfree(d_tcrec_);
+  for (cudaEvent_t e : fix_ev_) cudaEventDestroy(e);
+  fix_ev_.clear();
+  if (fix_stream_) cudaStreamDestroy(fix_stream_);
+  fix_stream_ = nullptr;
   if (h_err_) cudaFreeHost(h_err_);
   d_ctaps_ = nullptr;
   d_ctab_ = nullptr;
@@ -861,6 +865,12 @@ int PolyEngine::build_tc(int fmt) {
   if (err == cudaSuccess) err = dalloc(reinterpret_cast<void**>(&d_ctab_), tab.size() * sizeof(float2*));
   if (err == cudaSuccess) err = cudaMemcpy(d_ctab_, tab.data(), tab.size() * sizeof(float2*), cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = dalloc(reinterpret_cast<void**>(&d_tcrec_), sizeof(TcLaunch));
+  if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&fix_stream_, cudaStreamNonBlocking);
+  for (int i = 0; i <= kTcMaxGroups && err == cudaSuccess; ++i) {  // packs <= groups
+    cudaEvent_t e = nullptr;
+    err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (err == cudaSuccess) fix_ev_.push_back(e);
+  }
   if (err == cudaSuccess) err = cudaHostAlloc(&h_err_, sizeof(int), cudaHostAllocMapped);
   if (err == cudaSuccess) {
     *h_err_ = 0;
@@ -986,6 +996,11 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
   }
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return FDSP_ERR_UNSUPPORTED;
+  // the exact pass of pack li runs on fix_stream_ while pack li + 1's filter
+  // bank runs (they write different channels); the caller's stream joins it
+  // after the last pack (before the history update)
+  // (stream and events made by build_tc, outside any stream capture)
+  if (!fix_stream_ || fix_ev_.size() < plans.size() + 1) return FDSP_ERR_UNSUPPORTED;
   static thread_local TcLaunch L;
   for (size_t li = 0; li < plans.size(); ++li) {
     const TcPlan& plan = plans[li];
@@ -1080,15 +1095,21 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
       work = std::max<int64_t>(work, fast ? ((int64_t)S.J * Dp + S.T) / nc.rollover + 1 : (int64_t)S.J);
     }
     const unsigned fix_y = (unsigned)std::min<int64_t>(4096, (work + 511) / 512);
-    tc_fix_kernel<<<dim3((unsigned)plan.slots.size(), fix_y), 128, 0, stream>>>(L);
+    FDSP_TRY(cuda_status(cudaEventRecord(fix_ev_[li], stream)));
+    FDSP_TRY(cuda_status(cudaStreamWaitEvent(fix_stream_, fix_ev_[li], 0)));
+    tc_fix_kernel<<<dim3((unsigned)plan.slots.size(), fix_y), 128, 0, fix_stream_>>>(L);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     tc_groups_last_ += (int)packs[li].size();
+    if (li + 1 == plans.size()) {  // join
+      FDSP_TRY(cuda_status(cudaEventRecord(fix_ev_[plans.size()], fix_stream_)));
+      FDSP_TRY(cuda_status(cudaStreamWaitEvent(stream, fix_ev_[plans.size()], 0)));
+    }
     if (done_fn_) {
       std::vector<int> egs;
       for (int gi : packs[li]) egs.push_back(gmap[gi]);
-      notify_done(egs, stream);
+      notify_done(egs, fix_stream_);
     }
   }
   return FDSP_OK;

@@ -348,6 +348,8 @@ class PolyEngine {
   size_t xhl_cap_ = 0;                 // samples
   uint8_t* d_bbuf_ = nullptr;          // scratch: B images of the current apply
   TcLaunch* d_tcrec_ = nullptr;        // device copy of the current tensor-core launch record
+  cudaStream_t fix_stream_ = nullptr;  // exact rotation passes, beside the next packs' filter banks
+  std::vector<cudaEvent_t> fix_ev_;    // fork (one per pack) and join events
   size_t bbuf_cap_ = 0;
   int* h_err_ = nullptr;               // bounded-wait failures, mapped host memory
   int* d_err_ = nullptr;               // its device address
