@@ -490,56 +490,28 @@ DevPool::~DevPool() {
 
 int DevPool::init(size_t bytes) {
   std::lock_guard<std::mutex> lk(mu_);
-  if (base_ || bytes == 0) return FDSP_ERR_INVALID_ARG;
-  bytes &= ~(size_t)255;
+  if (base_ || bytes < RangePool::kAlign) return FDSP_ERR_INVALID_ARG;
+  bytes &= ~(RangePool::kAlign - 1);
   const cudaError_t e = cudaMalloc(&base_, bytes);
   if (e != cudaSuccess) {
     base_ = nullptr;
     return cuda_status(e);
   }
-  size_ = bytes;
-  free_.clear();
-  used_.clear();
-  free_[0] = bytes;
+  ranges_.init(bytes);
   return FDSP_OK;
 }
 
 void* DevPool::alloc(size_t bytes) {
-  const size_t n = (std::max<size_t>(bytes, 1) + 255) & ~(size_t)255;
   std::lock_guard<std::mutex> lk(mu_);
-  for (auto it = free_.begin(); it != free_.end(); ++it) {
-    if (it->second < n) continue;
-    const size_t off = it->first, len = it->second;
-    free_.erase(it);
-    if (len > n) free_[off + n] = len - n;
-    used_[off] = n;
-    return base_ + off;
-  }
-  return nullptr;
+  if (!base_) return nullptr;
+  const size_t off = ranges_.alloc(bytes);
+  return off == RangePool::kNone ? nullptr : base_ + off;
 }
 
 void DevPool::release(void* p) {
   if (!p) return;
   std::lock_guard<std::mutex> lk(mu_);
-  const size_t off = (size_t)(static_cast<char*>(p) - base_);
-  auto u = used_.find(off);
-  if (u == used_.end()) return;
-  size_t start = off, len = u->second;
-  used_.erase(u);
-  auto nx = free_.lower_bound(start);
-  if (nx != free_.end() && nx->first == start + len) {  // merge with the next free range
-    len += nx->second;
-    nx = free_.erase(nx);
-  }
-  if (nx != free_.begin()) {  // and with the previous one
-    auto pv = std::prev(nx);
-    if (pv->first + pv->second == start) {
-      start = pv->first;
-      len += pv->second;
-      free_.erase(pv);
-    }
-  }
-  free_[start] = len;
+  if (base_) ranges_.release((size_t)(static_cast<char*>(p) - base_));
 }
 
 static int choose_qt(uint32_t D, int tmax) {

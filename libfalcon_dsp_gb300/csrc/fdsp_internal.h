@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "fdsp_c.h"
+#include "fdsp_pool.h"
 #include "fdsp_tc_plan.h"
 
 #define FDSP_TRY(expr)              \
@@ -183,9 +184,9 @@ struct EngineChannel {
   NcoConst nco;
 };
 
-// Device memory pool: one cudaMalloc'd region handed out first-fit (256-byte
-// aligned, neighbours coalesced on release; host-side bookkeeping under a
-// mutex).  The stream server gives it to its channelizers so that opening,
+// Device memory pool: one cudaMalloc'd region handed out by a RangePool
+// (fdsp_pool.h: first fit, 256-byte aligned, neighbours coalesced) under a
+// mutex.  The stream server gives it to its channelizers so that opening,
 // closing and resetting streams allocate nothing from the driver.
 class DevPool {
  public:
@@ -193,13 +194,11 @@ class DevPool {
   int init(size_t bytes);            // the one cudaMalloc
   void* alloc(size_t bytes);         // nullptr when no free range fits
   void release(void* p);
-  size_t size() const { return size_; }
+  size_t size() const { return ranges_.size(); }
 
  private:
   char* base_ = nullptr;
-  size_t size_ = 0;
-  std::map<size_t, size_t> free_;    // offset -> bytes
-  std::map<size_t, size_t> used_;    // offset -> bytes
+  RangePool ranges_;
   std::mutex mu_;
 };
 
