@@ -101,9 +101,11 @@ struct PolyLaunch {
 };
 
 // ---------------------------------------------------------------------------
-// Tensor-core launch: every decimation group computed on the tensor cores,
-// planned by tc_plan (fdsp_tc_plan.h).  The whole record travels in the
-// kernel parameter block (no host->device copy per apply).
+// Tensor-core launch: the decimation groups of one launch pack computed on
+// the tensor cores, planned by tc_plan (fdsp_tc_plan.h).  The record is the
+// parameter block of tc_prep_kernel and tc_fix_kernel (no host->device copy
+// per apply); tc_prep_kernel copies it into device memory for the filter-bank
+// kernel, which takes only the tensor maps and a pointer (TcFilterParams).
 // ---------------------------------------------------------------------------
 struct TcLaunch {
   CUtensorMap maps[kTcMaxGroups];    // A operand of each group: rows D' samples apart over xhl
