@@ -64,7 +64,9 @@
 
 namespace fdsp {
 
-constexpr int kTcEpiWarps = 16;                       // four per TMEM lane quarter
+constexpr int kTcEpiWarps = 16;                       // kTcEpiPerQ per TMEM lane quarter
+constexpr int kTcEpiPerQ = kTcEpiWarps / 4;
+constexpr int kTcEpiOwn = 8 / kTcEpiPerQ;             // most column chunks a warp reads per item (R NS <= 64)
 constexpr int kTcSchedWarp = 2 + kTcEpiWarps;         // the item scheduler (after the epilogue warps)
 constexpr int kTcThreads = 96 + 32 * kTcEpiWarps;     // producer, MMA, epilogue and scheduler warps
 constexpr int kTcRing = 16;                           // items announced ahead (> stages + 2)
@@ -662,7 +664,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
   } else {
     // ------------------------------------------------------------ epilogue
     const int q = warp & 3;           // TMEM lane quarter this warp may read
-    const int h = (warp - 2) >> 2;    // which of the item's column chunks (every fourth)
+    const int h = (warp - 2) >> 2;    // which of the item's column chunks (every kTcEpiPerQ-th)
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     bool failed = false;
     for (int k = 0;; ++k) {
@@ -681,15 +683,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
       const int R = M.R, NS = M.NS, nch = NS >> 3;
       const int64_t D = s_groups[M.group].D;
       const uint32_t laneD = (uint32_t)lane * (uint32_t)D;
-      // every column chunk this warp owns (at most two: R * NS <= 64) is read
-      // out of tensor memory first and the accumulator slot released, so the
-      // MMAs of a later item run while this warp rotates and stores
-      const int n_own = (R * nch - h + 3) >> 2;  // chunks h, h + 4 (0, 1 or 2)
-      float ya[16], yb[16];                      // (hi + lo) sums of the two chunks
+      // every column chunk this warp owns (at most kTcEpiOwn: R * NS <= 64)
+      // is read out of tensor memory first and the accumulator slot
+      // released, so the MMAs of a later item run while this warp rotates
+      // and stores
+      const int n_own = (R * nch - h + kTcEpiPerQ - 1) / kTcEpiPerQ;  // chunks h, h + kTcEpiPerQ, ...
+      float yv[kTcEpiOwn][16];                                       // (hi + lo) sums of those chunks
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
+      for (int u = 0; u < kTcEpiOwn; ++u) {
         if (u < n_own) {
-          const int idx = h + 4 * u;
+          const int idx = h + kTcEpiPerQ * u;
           const int r = idx / nch, cc = idx - r * nch;
           const uint32_t col = tbase + lane_off + (uint32_t)a * 256u + (uint32_t)(r * (256 / R) + 16 * cc);
           uint32_t vh[16], vl[16];
@@ -697,21 +700,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
           tc::tmem_ld16(col + (uint32_t)(2 * NS), vl);
           tc::tmem_wait_ld();
 #pragma unroll
-          for (int i = 0; i < 16; ++i) (u == 0 ? ya : yb)[i] = __uint_as_float(vh[i]) + __uint_as_float(vl[i]);
+          for (int i = 0; i < 16; ++i) yv[u][i] = __uint_as_float(vh[i]) + __uint_as_float(vl[i]);
         }
       }
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acc_empty[a]);
       // one copy of the chunk code (kept small: the warps of every role share
-      // the SM's instruction cache); the second chunk moves into ya after the first
+      // the SM's instruction cache); the chunks move down into yv[0] in turn
 #pragma unroll 1
       for (int u = 0; u < n_own; ++u) {
         if (u > 0) {
 #pragma unroll
-          for (int i = 0; i < 16; ++i) ya[i] = yb[i];
+          for (int w = 0; w + 1 < kTcEpiOwn; ++w)
+#pragma unroll
+            for (int i = 0; i < 16; ++i) yv[w][i] = yv[w + 1][i];
         }
-        const int idx = h + 4 * u;
+        const int idx = h + kTcEpiPerQ * u;
         const int r = idx / nch, cc = idx - r * nch;
         const int64_t row0 = ((int64_t)t * R + r) * kTcRows + q * 32;  // row of lane 0
         const int64_t j = row0 + lane;
@@ -746,7 +751,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
             const uint4 A = k2 ? a1 : a0, Bv = k2 ? b1 : b0;
             const uint32_t Rr = Bv.x, Tm1 = Bv.z >> 16, om_lo = A.z, om_hi = A.w;
             const uint32_t P0 = __shfl_sync(0xffffffffu, p0, e + k2);
-            const float2 y0 = make_float2(ya[2 * (e + k2)], ya[2 * (e + k2) + 1]);
+            const float2 y0 = make_float2(yv[0][2 * (e + k2)], yv[0][2 * (e + k2) + 1]);
             uint32_t pc = P0 + laneD;
             pc = pc >= Rr ? pc - Rr : pc;
             const bool fast = pc + Tm1 < Rr || (om_lo | om_hi) == 0u;
