@@ -457,6 +457,7 @@ NcoConst make_nco(uint32_t fs, int32_t f) {
 
 PolyEngine::~PolyEngine() {
   if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  if (graph_) cudaGraphDestroy(graph_);
   for (auto e : kprof_ev_)
     if (e) cudaEventDestroy(e);
   free_tc();
@@ -769,9 +770,12 @@ void PolyEngine::notify_done(const std::vector<int>& egroups, cudaStream_t strea
 void PolyEngine::set_graph(bool on) {
   use_graph_ = on;
   graph_replays_ = 0;
-  if (!on && graph_exec_) {
-    cudaGraphExecDestroy(graph_exec_);
+  if (!on) {
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
     graph_exec_ = nullptr;
+    if (graph_) cudaGraphDestroy(graph_);
+    graph_ = nullptr;
+    knodes_.clear();
   }
 }
 
@@ -1046,9 +1050,10 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
         if (e != cudaSuccess) return cuda_status(e);
         if (kprof_) cudaEventRecord(kprof_event(), stream);
-        kern<<<dim3((unsigned)ftiles, (unsigned)(nm - first)), kThreads, fsmem, stream>>>(L, -1 - first);
+        int garg = -1 - first;
+        e = klaunch(reinterpret_cast<const void*>(kern), dim3((unsigned)ftiles, (unsigned)(nm - first)),
+                    dim3(kThreads), fsmem, stream, L, garg);
         if (kprof_) cudaEventRecord(kprof_event(), stream);
-        e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_status(e);
         launches_last_++;
         if (done_fn_) {
@@ -1076,18 +1081,23 @@ int PolyEngine::launch(const float2* d_in, uint64_t n, float2* const* out, cudaS
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e);
     if (kprof_) cudaEventRecord(kprof_event(), stream);
-    kern<<<(unsigned)gd.ntiles, kThreads, smem, stream>>>(L, gi);
+    int garg = gi;
+    e = klaunch(reinterpret_cast<const void*>(kern), dim3((unsigned)gd.ntiles), dim3(kThreads), smem, stream, L, garg);
     if (kprof_) cudaEventRecord(kprof_event(), stream);
-    e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     if (!prof_ev_.empty()) cudaEventRecord(prof_ev_[2 * eg + 1], stream);
     if (done_fn_) notify_done(std::vector<int>(1, eg), stream);
   }
   if (H_ > 0) {
-    hist_update_kernel<<<(H_ + 255) / 256, 256, 0, stream>>>(d_hist_[hist_cur_], in16_ ? nullptr : d_in, in16_,
-                                                              (int64_t)n, H_, d_hist_[hist_cur_ ^ 1]);
-    cudaError_t e = cudaGetLastError();
+    const float2* a0 = d_hist_[hist_cur_];
+    const float2* a1 = in16_ ? nullptr : d_in;
+    const short2* a2 = in16_;
+    int64_t a3 = (int64_t)n;
+    int a4 = H_;
+    float2* a5 = d_hist_[hist_cur_ ^ 1];
+    cudaError_t e = klaunch(reinterpret_cast<const void*>(hist_update_kernel), dim3((unsigned)((H_ + 255) / 256)),
+                            dim3(256), 0, stream, a0, a1, a2, a3, a4, a5);
     if (e != cudaSuccess) return cuda_status(e);
     hist_cur_ ^= 1;
     launches_last_++;
@@ -1122,35 +1132,79 @@ int PolyEngine::apply(const float2* d_in, uint64_t n, float2* const* out, const 
   const bool graph = use_graph_ && !kprof_ && !done_fn_ && stream != nullptr &&
                      cudaStreamIsCapturing(stream, &capturing) == cudaSuccess &&
                      capturing == cudaStreamCaptureStatusNone;
-  if (graph) {
-    const cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed);
-    if (e != cudaSuccess) return cuda_status(e);
-  }
-  int st;
-  switch (nb_) {
-    case 1: st = launch<1>(d_in, n, out, stream); break;
-    case 2: st = launch<2>(d_in, n, out, stream); break;
-    case 4: st = launch<4>(d_in, n, out, stream); break;
-    default: st = launch<8>(d_in, n, out, stream); break;
-  }
-  if (graph) {
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(stream, &g);
-    if (st == FDSP_OK && e != cudaSuccess) st = cuda_status(e);
-    if (st == FDSP_OK && graph_exec_) {
-      // same launch sequence shape: only kernel parameters and grids change
-      cudaGraphExecUpdateResultInfo info;
-      if (cudaGraphExecUpdate(graph_exec_, g, &info) != cudaSuccess) {
-        cudaGetLastError();
-        cudaGraphExecDestroy(graph_exec_);
-        graph_exec_ = nullptr;
-      }
+  auto run = [&]() {
+    switch (nb_) {
+      case 1: return launch<1>(d_in, n, out, stream);
+      case 2: return launch<2>(d_in, n, out, stream);
+      case 4: return launch<4>(d_in, n, out, stream);
+      default: return launch<8>(d_in, n, out, stream);
     }
-    if (st == FDSP_OK && !graph_exec_) {
-      e = cudaGraphInstantiate(&graph_exec_, g, 0);
+  };
+  int st = FDSP_OK;
+  bool done = false;
+  if (graph && graph_exec_ && !knodes_.empty()) {
+    // replay: the same launch sequence with this apply's arguments written
+    // into the recorded kernel nodes (no capture)
+    const int hist_save = hist_cur_;
+    kmode_ = 2;
+    kcur_ = 0;
+    kshape_ok_ = true;
+    st = run();
+    kmode_ = 0;
+    if (st != FDSP_OK) return st;
+    if (kshape_ok_ && kcur_ == knodes_.size()) {
+      const cudaError_t e = cudaGraphLaunch(graph_exec_, stream);
+      if (e != cudaSuccess) return cuda_status(e);
+      graph_replays_++;
+      done = true;
+    } else {  // another launch sequence: capture it afresh
+      hist_cur_ = hist_save;
+      launches_last_ = 0;
+      tc_groups_last_ = 0;
+    }
+  }
+  if (!done && graph) {
+    cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return cuda_status(e);
+    kmode_ = 1;
+    knodes_.clear();
+    kfuncs_.clear();
+    kshape_ok_ = true;
+    st = run();
+    kmode_ = 0;
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(stream, &g);
+    if (st == FDSP_OK && e != cudaSuccess) st = cuda_status(e);
+    if (st == FDSP_OK && kshape_ok_) {
+      // a fresh executable graph whose kernel nodes the next applies update
+      if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+      graph_exec_ = nullptr;
+      if (graph_) cudaGraphDestroy(graph_);
+      graph_ = g;
+      g = nullptr;
+      e = cudaGraphInstantiate(&graph_exec_, graph_, 0);
       if (e != cudaSuccess) {
         graph_exec_ = nullptr;
+        knodes_.clear();
         st = cuda_status(e);
+      }
+    } else if (st == FDSP_OK) {
+      // nodes not recorded: update the executable graph from each capture
+      knodes_.clear();
+      if (graph_exec_) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(graph_exec_, g, &info) != cudaSuccess) {
+          cudaGetLastError();
+          cudaGraphExecDestroy(graph_exec_);
+          graph_exec_ = nullptr;
+        }
+      }
+      if (!graph_exec_) {
+        e = cudaGraphInstantiate(&graph_exec_, g, 0);
+        if (e != cudaSuccess) {
+          graph_exec_ = nullptr;
+          st = cuda_status(e);
+        }
       }
     }
     if (st == FDSP_OK) {
@@ -1159,7 +1213,9 @@ int PolyEngine::apply(const float2* d_in, uint64_t n, float2* const* out, const 
       else graph_replays_++;
     }
     if (g) cudaGraphDestroy(g);
+    done = true;
   }
+  if (!done) st = run();
   if (st != FDSP_OK) return st;
   // advance the streaming state (polyphase_resampler.cc:303-312)
   for (auto& k : classes_) polyphase_advance(k.up, k.down, k.phase, k.xoffset, n, k.M);

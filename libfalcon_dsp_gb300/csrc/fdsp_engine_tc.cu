@@ -1069,8 +1069,9 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     const int nb_build = std::max(1, std::min(num_sms_, (pieces + 255) / 256));
     const int64_t nb_split = li == 0 ? std::min<int64_t>((xhl_need + 255) / 256, (int64_t)num_sms_ * 8) : 0;
     auto prep = tc_fmt_ == 0 ? tc_prep_kernel<0> : tc_prep_kernel<1>;
-    prep<<<(unsigned)(nb_build + nb_split), 256, 0, stream>>>(L, nb_build);
-    cudaError_t e = cudaGetLastError();
+    int nbb = nb_build;
+    cudaError_t e = klaunch(reinterpret_cast<const void*>(prep), dim3((unsigned)(nb_build + nb_split)), dim3(256), 0,
+                            stream, L, nbb);
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     auto kern = tc_fmt_ == 0 ? tc_filter_kernel<0> : tc_filter_kernel<1>;
@@ -1080,9 +1081,9 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     static thread_local TcFilterParams FP;
     std::memcpy(FP.maps, L.maps, sizeof(FP.maps));
     FP.rec = d_tcrec_;
-    kern<<<(unsigned)plan.G, kTcThreads, (size_t)plan.smem, stream>>>(FP);
+    e = klaunch(reinterpret_cast<const void*>(kern), dim3((unsigned)plan.G), dim3(kTcThreads), (size_t)plan.smem, stream,
+                FP);
     if (kprof_) cudaEventRecord(kprof_event(), stream);
-    e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     // exact pass: blocks per slot for the most rows (or rollover points) a
@@ -1100,16 +1101,16 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
       work = std::max<int64_t>(work, fast ? ((int64_t)S.J * Dp + S.T) / nc.rollover + 1 : (int64_t)S.J);
     }
     const unsigned fix_y = (unsigned)std::min<int64_t>(4096, (work + 511) / 512);
-    FDSP_TRY(cuda_status(cudaEventRecord(fix_ev_[li], stream)));
-    FDSP_TRY(cuda_status(cudaStreamWaitEvent(fix_stream_, fix_ev_[li], 0)));
-    tc_fix_kernel<<<dim3((unsigned)plan.slots.size(), fix_y), 128, 0, fix_stream_>>>(L);
-    e = cudaGetLastError();
+    FDSP_TRY(cuda_status(krecord(fix_ev_[li], stream)));
+    FDSP_TRY(cuda_status(kwait(fix_stream_, fix_ev_[li])));
+    e = klaunch(reinterpret_cast<const void*>(tc_fix_kernel), dim3((unsigned)plan.slots.size(), fix_y), dim3(128), 0,
+                fix_stream_, L);
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     tc_groups_last_ += (int)packs[li].size();
     if (li + 1 == plans.size()) {  // join
-      FDSP_TRY(cuda_status(cudaEventRecord(fix_ev_[plans.size()], fix_stream_)));
-      FDSP_TRY(cuda_status(cudaStreamWaitEvent(stream, fix_ev_[plans.size()], 0)));
+      FDSP_TRY(cuda_status(krecord(fix_ev_[plans.size()], fix_stream_)));
+      FDSP_TRY(cuda_status(kwait(stream, fix_ev_[plans.size()])));
     }
     if (done_fn_) {
       std::vector<int> egs;

@@ -378,8 +378,59 @@ class PolyEngine {
   int tc_groups_last_ = 0;
   int force_ = -1;                     // autotuning: -1 chosen forms, 0 all FP32, 1 all tensor cores
   bool use_graph_ = false;
+  cudaGraph_t graph_ = nullptr;        // the captured launch sequence behind graph_exec_
   cudaGraphExec_t graph_exec_ = nullptr;
   int graph_replays_ = 0;              // applies replayed as a graph since set_graph(true)
+  // Kernel launches of an apply go through klaunch: direct (kmode_ 0), or
+  // while the sequence is captured (1: each kernel node is recorded in
+  // launch order), or for a replay (2: each launch's arguments are written
+  // into its recorded node of graph_exec_ instead: no capture per apply).
+  int kmode_ = 0;
+  std::vector<cudaGraphNode_t> knodes_;
+  std::vector<const void*> kfuncs_;    // the kernel of each recorded node (a replay needs the same sequence)
+  size_t kcur_ = 0;
+  bool kshape_ok_ = true;
+ public:
+  template <class... A>
+  cudaError_t klaunch(const void* func, dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&... args) {
+    void* ptrs[] = {static_cast<void*>(&args)...};
+    if (kmode_ == 2) {
+      if (kcur_ >= knodes_.size() || kfuncs_[kcur_] != func) {
+        kshape_ok_ = false;
+        return cudaSuccess;
+      }
+      cudaKernelNodeParams p = {};
+      p.func = const_cast<void*>(func);
+      p.gridDim = grid;
+      p.blockDim = block;
+      p.sharedMemBytes = (unsigned)smem;
+      p.kernelParams = ptrs;
+      if (cudaGraphExecKernelNodeSetParams(graph_exec_, knodes_[kcur_++], &p) != cudaSuccess) {
+        cudaGetLastError();
+        kshape_ok_ = false;
+      }
+      return cudaSuccess;
+    }
+    cudaError_t e = cudaLaunchKernel(func, grid, block, ptrs, smem, s);
+    if (e == cudaSuccess && kmode_ == 1) {
+      cudaStreamCaptureStatus cs;
+      const cudaGraphNode_t* deps = nullptr;
+      size_t nd = 0;
+      e = cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+      if (e == cudaSuccess && nd == 1) {
+        knodes_.push_back(deps[0]);
+        kfuncs_.push_back(func);
+      } else {
+        kshape_ok_ = false;  // (the replay needs one node per launch)
+      }
+      e = cudaSuccess;
+    }
+    return e;
+  }
+  // stream-order edges of an apply (skipped in a replay: they are graph edges)
+  cudaError_t krecord(cudaEvent_t ev, cudaStream_t s) { return kmode_ == 2 ? cudaSuccess : cudaEventRecord(ev, s); }
+  cudaError_t kwait(cudaStream_t s, cudaEvent_t ev) { return kmode_ == 2 ? cudaSuccess : cudaStreamWaitEvent(s, ev, 0); }
+ private:
   bool use_tc_for(int eg) const;
   std::vector<cudaEvent_t> prof_ev_;   // autotuning: [2 g] / [2 g + 1] around group g
   std::vector<int> prof_hit_;          // group g launched in the timed apply
