@@ -228,11 +228,12 @@ int fdsp_channelizer_autotune(fdsp_channelizer *h, uint64_t n_in, fdsp_stream_t 
  * tensor-core form for it. */
 int fdsp_channelizer_num_groups(const fdsp_channelizer *h, uint32_t *n);
 /* CUDA-graph replay of every later apply (no counterpart in the reference):
- * each apply's launches are captured on the caller's stream and replayed as
- * one graph, whose instantiation is updated in place while the launch
- * sequence keeps its shape.  Applies on the legacy default stream (NULL), or
- * on a stream the caller is itself capturing, launch directly.  `replays`
- * (may be NULL) receives the applies replayed since graphs were enabled. */
+ * the first apply's launches are captured on the caller's stream and
+ * instantiated once; later applies write their kernels' arguments into that
+ * graph's nodes (no capture) and replay it, and a different launch sequence
+ * is captured afresh.  Applies on the legacy default stream (NULL), or on a
+ * stream the caller is itself capturing, launch directly.  `replays` (may be
+ * NULL) receives the applies replayed since graphs were enabled. */
 int fdsp_channelizer_set_graph(fdsp_channelizer *h, int enable);
 int fdsp_channelizer_graph_replays(const fdsp_channelizer *h, uint32_t *replays);
 int fdsp_channelizer_group_info(const fdsp_channelizer *h, uint32_t group, uint32_t *down_rate, uint32_t *tile_rows,

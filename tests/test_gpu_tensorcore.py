@@ -130,6 +130,42 @@ def test_tc_row_split_matches_fp64(split):
     assert g.tc_groups() == len(info)
 
 
+@pytest.mark.parametrize("mode", ["fp32", "fp16x3"])
+def test_graph_recaptures_when_the_launch_sequence_changes(mode):
+    """The graph is captured once and later applies only rewrite its kernel
+    nodes; block sizes that change the launch sequence (tile counts, tiny
+    blocks where some groups emit nothing, a precision switch) make it
+    capture afresh.  Every apply equals direct launches bit for bit."""
+    torch = pytest.importorskip("torch")
+    fs = 61440000
+    chans = channelizer_256_plan(float(fs), [1.5e6, -4.0e6, 8.5e6], 24, 13)
+    sizes = [50000, 50000, 3, 50000, 700, 131072, 131072, 1, 50000]
+    x, _ = tone_signal(sum(sizes), float(fs), 48, seed=14)
+    xd = torch.from_numpy(x).cuda()
+    outs = {}
+    for graph in (False, True):
+        g = F.MultiRateChannelizerCuda(fs, chans)
+        g.set_precision(mode)
+        g.set_graph(graph)
+        s = torch.cuda.Stream()
+        ys, n0 = [], 0
+        with torch.cuda.stream(s):
+            for i, n in enumerate(sizes):
+                if i == 6:  # switch the form mid-stream and back
+                    g.set_precision("fp32" if mode != "fp32" else "fp16x3")
+                if i == 7:
+                    g.set_precision(mode)
+                ys.append([y.clone() for y in g.apply(xd[n0:n0 + n])])
+                n0 += n
+        s.synchronize()
+        outs[graph] = [[y.cpu().numpy() for y in blk] for blk in ys]
+        if graph:
+            assert g.graph_replays() == len(sizes)
+    for a, b in zip(outs[False], outs[True]):
+        for ya, yb in zip(a, b):
+            assert np.array_equal(ya, yb)
+
+
 def test_autotune_keeps_results_and_streaming():
     """The autotuner only picks tile heights and forms: outputs after it stay
     within the tensor-core bound of the FP64 oracle, from a reset state, and
