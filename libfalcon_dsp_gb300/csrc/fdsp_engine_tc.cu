@@ -1,8 +1,9 @@
 // Tensor-core form of the polyphase engine (tcgen05 + TMA, sm_103a).
 //
-// The fused shift + polyphase contraction of every decimation group of an
-// apply runs as one persistent launch of matrix products over 128-row tiles
-// (the planner, fdsp_tc_plan.h, describes the operands):
+// The fused shift + polyphase contraction of the decimation groups of an
+// apply runs as persistent launches of matrix products over 128-row tiles,
+// one per launch pack (as many groups as the launch records hold; the
+// planner, fdsp_tc_plan.h, describes the operands):
 //
 //     Y[j][n] = sum_k A[j][k] B[k][n]
 //
