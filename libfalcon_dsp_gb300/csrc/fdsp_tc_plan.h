@@ -127,8 +127,9 @@ struct TcSlotX {
 // A bundle: every slot of one channel under row split S, in output order
 // (offset r + b U = 0 .. U S - 1), so that row j of the bundle holds the
 // channel's consecutive outputs U S j .. U S j + U S - 1 and the epilogue
-// writes them as contiguous pairs.  Its width is its slot count rounded up
-// to even (pairs never straddle two bundles).
+// writes them as contiguous pairs (a slot at an even position of its merge
+// set and the next one of the same bundle).  Its width is its slot count:
+// bundles sit back to back, a one-slot bundle takes one column pair.
 struct TcBundle {
   std::vector<TcSlotX> slots;
   int64_t start;  // earliest window start of its slots
@@ -166,7 +167,7 @@ inline std::vector<TcBundle> tc_bundles(const TcGroupIn& g, int S) {
       b.slots.push_back(xs[j]);
       ++j;
     }
-    b.width = (int)((b.slots.size() + 1) & ~(size_t)1);
+    b.width = (int)b.slots.size();
     bs.push_back(b);
     i = j;
   }
@@ -297,6 +298,7 @@ inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_
       int64_t Jmax = 0;
       for (size_t q = i; q < j; ++q) {
         const TcBundle& b = bs[q];
+        const size_t pos0 = p.slots.size() - (size_t)m.slot0;  // the bundle's first position in the merge set
         for (size_t k = 0; k < b.slots.size(); ++k) {
           const TcSlotX& x = b.slots[k];
           TcSlot s{};
@@ -307,15 +309,12 @@ inline int tc_plan(const std::vector<TcGroupIn>& gin, int64_t N, int H, int num_
           s.U = (uint16_t)x.s.U;
           s.o = (uint16_t)(x.start + H - a);
           s.phi = (uint16_t)x.s.phi;
-          // even slot followed by the channel's next output: one 16-byte store
-          s.flags = (k % 2 == 0 && k + 1 < b.slots.size() && b.slots[k + 1].s.r == x.s.r + 1) ? 1 : 0;
+          // a slot at an even position followed by the channel's next output:
+          // one 16-byte store
+          s.flags = ((pos0 + k) % 2 == 0 && k + 1 < b.slots.size() && b.slots[k + 1].s.r == x.s.r + 1) ? 1 : 0;
           p.slots.push_back(s);
           p.slot_r.push_back(x.s.r);
           Jmax = std::max(Jmax, x.s.J);
-        }
-        if (b.slots.size() & 1) {
-          p.slots.push_back(TcSlot{});
-          p.slot_r.push_back(0);
         }
       }
       for (int q = width; q < NS; ++q) {
