@@ -742,10 +742,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_filter_kernel(const __grid_c
         const uint32_t e8 = tc::smem_u32(E8);
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
-          const uint4 a0 = lds128(e8 + (uint32_t)e * kTcEpiSlotBytes);
           const uint4 b0 = lds128(e8 + (uint32_t)e * kTcEpiSlotBytes + 32u);
-          const uint4 a1 = lds128(e8 + (uint32_t)(e + 1) * kTcEpiSlotBytes);
           const uint4 b1 = lds128(e8 + (uint32_t)(e + 1) * kTcEpiSlotBytes + 32u);
+          if ((int32_t)b0.y <= 0 && (int32_t)b1.y <= 0) continue;  // two padding slots (no rows): nothing to do
+          const uint4 a0 = lds128(e8 + (uint32_t)e * kTcEpiSlotBytes);
+          const uint4 a1 = lds128(e8 + (uint32_t)(e + 1) * kTcEpiSlotBytes);
           float2 o[2];
 #pragma unroll
           for (int k2 = 0; k2 < 2; ++k2) {
