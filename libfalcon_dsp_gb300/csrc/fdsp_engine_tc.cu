@@ -813,10 +813,10 @@ void PolyEngine::free_tc() {
   if (d_xhl_) dfree(d_xhl_);
   if (d_bbuf_) dfree(d_bbuf_);
   if (d_tcrec_) dfree(d_tcrec_);
-  for (cudaEvent_t e : fix_ev_) cudaEventDestroy(e);
-  fix_ev_.clear();
-  if (fix_stream_) cudaStreamDestroy(fix_stream_);
-  fix_stream_ = nullptr;
+  for (cudaEvent_t e : pack_ev_) cudaEventDestroy(e);
+  pack_ev_.clear();
+  for (cudaStream_t q : side_) cudaStreamDestroy(q);
+  side_.clear();
   if (h_err_) cudaFreeHost(h_err_);
   d_ctaps_ = nullptr;
   d_ctab_ = nullptr;
@@ -871,12 +871,17 @@ int PolyEngine::build_tc(int fmt) {
   for (size_t c = 0; c < chans_.size(); ++c) tab[c] = d_ctaps_ + off[c];
   if (err == cudaSuccess) err = dalloc(reinterpret_cast<void**>(&d_ctab_), tab.size() * sizeof(float2*));
   if (err == cudaSuccess) err = cudaMemcpy(d_ctab_, tab.data(), tab.size() * sizeof(float2*), cudaMemcpyHostToDevice);
-  if (err == cudaSuccess) err = dalloc(reinterpret_cast<void**>(&d_tcrec_), sizeof(TcLaunch));
-  if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&fix_stream_, cudaStreamNonBlocking);
-  for (int i = 0; i <= kTcMaxGroups && err == cudaSuccess; ++i) {  // packs <= groups
+  // one device record per launch pack (packs <= groups)
+  if (err == cudaSuccess) err = dalloc(reinterpret_cast<void**>(&d_tcrec_), kTcMaxGroups * sizeof(TcLaunch));
+  for (int i = 0; i < kTcSideStreams && err == cudaSuccess; ++i) {
+    cudaStream_t q = nullptr;
+    err = cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking);
+    if (err == cudaSuccess) side_.push_back(q);
+  }
+  for (int i = 0; i <= kTcSideStreams && err == cudaSuccess; ++i) {
     cudaEvent_t e = nullptr;
     err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
-    if (err == cudaSuccess) fix_ev_.push_back(e);
+    if (err == cudaSuccess) pack_ev_.push_back(e);
   }
   if (err == cudaSuccess) err = cudaHostAlloc(&h_err_, sizeof(int), cudaHostAllocMapped);
   if (err == cudaSuccess) {
@@ -897,10 +902,16 @@ int PolyEngine::tc_error() {
 
 // Plans and enqueues the tensor-core form of the groups in `tc_groups`
 // (engine group indices).  Groups are packed greedily into launches whose
-// records fit the kernel parameter block; per launch one prep (the first
-// also splits the input, which every launch then reads) and one
-// filter-bank launch.  Groups no launch can hold are returned in `fallback`
-// for the FP32 kernel.
+// records fit the kernel parameter block; per pack one prep (the first also
+// splits the input, which every pack then reads), one filter-bank launch and
+// the exact rotation pass.  Each pack has its own device record and B-image
+// region, so the packs run at the same time: pack 0 on the caller's stream,
+// pack k > 0 on side stream (k - 1) mod kTcSideStreams once the split is
+// done, and a pack's filter-bank CTAs take the SMs that the earlier packs'
+// CTAs leave as they finish (one launch's tail instead of one per pack).
+// With kernel timing on, the packs run one after another on the caller's
+// stream (each launch timed alone).  Groups no launch can hold are returned
+// in `fallback` for the FP32 kernel.
 int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, const std::vector<int>& tc_groups,
                           std::vector<int>& fallback, cudaStream_t stream) {
   fallback.clear();
@@ -979,13 +990,16 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     }
   }
   if (plans.empty()) return FDSP_OK;
-  // scratch: split input and B images (grow only; launches run in stream
-  // order, so they share one B buffer)
+  if (plans.size() > (size_t)kTcMaxGroups) return FDSP_ERR_UNSUPPORTED;
+  // scratch (grow only): the split input, which every pack reads, and the B
+  // images of every pack (a 1 KB aligned region each)
   int64_t xhl_need = 0;
   size_t b_need = 0;
-  for (const TcPlan& p : plans) {
-    xhl_need = std::max(xhl_need, p.xhl_samples);
-    b_need = std::max(b_need, p.b_bytes);
+  std::vector<size_t> boff(plans.size());
+  for (size_t li = 0; li < plans.size(); ++li) {
+    xhl_need = std::max(xhl_need, plans[li].xhl_samples);
+    boff[li] = b_need;
+    b_need += (plans[li].b_bytes + 1023u) & ~(size_t)1023u;
   }
   if ((size_t)xhl_need > xhl_cap_) {
     if (d_xhl_) dfree(d_xhl_);
@@ -1003,14 +1017,22 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
   }
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return FDSP_ERR_UNSUPPORTED;
-  // the exact pass of pack li runs on fix_stream_ while pack li + 1's filter
-  // bank runs (they write different channels); the caller's stream joins it
-  // after the last pack (before the history update)
-  // (stream and events made by build_tc, outside any stream capture)
-  if (!fix_stream_ || fix_ev_.size() < plans.size() + 1) return FDSP_ERR_UNSUPPORTED;
+  // (side streams and events made by build_tc, outside any stream capture)
+  if (side_.empty() || pack_ev_.size() < side_.size() + 1) return FDSP_ERR_UNSUPPORTED;
+  const bool concurrent = !kprof_ && plans.size() > 1;
+  std::vector<char> side_used(side_.size(), 0);
   static thread_local TcLaunch L;
   for (size_t li = 0; li < plans.size(); ++li) {
     const TcPlan& plan = plans[li];
+    cudaStream_t ps = stream;  // this pack's stream
+    if (concurrent && li > 0) {
+      const size_t si = (li - 1) % side_.size();
+      ps = side_[si];
+      if (!side_used[si]) {  // after the split (recorded below by pack 0)
+        FDSP_TRY(cuda_status(kwait(ps, pack_ev_[0])));
+        side_used[si] = 1;
+      }
+    }
     std::memset(&L, 0, sizeof(L));
     L.block = in16_ ? nullptr : d_in;
     L.block16 = in16_;
@@ -1018,9 +1040,9 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     L.nco = d_nco_;
     L.ctaps = d_ctab_;
     L.xhl = d_xhl_;
-    L.bbuf = d_bbuf_;
+    L.bbuf = d_bbuf_ + boff[li];
     L.err = d_err_;
-    L.rec_out = d_tcrec_;
+    L.rec_out = d_tcrec_ + li;
     L.N = (int64_t)n;
     L.Lc = plan.Lc;
     L.xhl_n = xhl_need;
@@ -1073,19 +1095,20 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     auto prep = tc_fmt_ == 0 ? tc_prep_kernel<0> : tc_prep_kernel<1>;
     int nbb = nb_build;
     cudaError_t e = klaunch(reinterpret_cast<const void*>(prep), dim3((unsigned)(nb_build + nb_split)), dim3(256), 0,
-                            stream, L, nbb);
+                            ps, L, nbb);
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
+    if (concurrent && li == 0) FDSP_TRY(cuda_status(krecord(pack_ev_[0], stream)));
     auto kern = tc_fmt_ == 0 ? tc_filter_kernel<0> : tc_filter_kernel<1>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, plan.smem);
     if (e != cudaSuccess) return cuda_status(e);
-    if (kprof_) cudaEventRecord(kprof_event(), stream);
+    if (kprof_) cudaEventRecord(kprof_event(), ps);
     static thread_local TcFilterParams FP;
     std::memcpy(FP.maps, L.maps, sizeof(FP.maps));
-    FP.rec = d_tcrec_;
-    e = klaunch(reinterpret_cast<const void*>(kern), dim3((unsigned)plan.G), dim3(kTcThreads), (size_t)plan.smem, stream,
+    FP.rec = d_tcrec_ + li;
+    e = klaunch(reinterpret_cast<const void*>(kern), dim3((unsigned)plan.G), dim3(kTcThreads), (size_t)plan.smem, ps,
                 FP);
-    if (kprof_) cudaEventRecord(kprof_event(), stream);
+    if (kprof_) cudaEventRecord(kprof_event(), ps);
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     // exact pass: blocks per slot for the most rows (or rollover points) a
@@ -1103,22 +1126,22 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
       work = std::max<int64_t>(work, fast ? ((int64_t)S.J * Dp + S.T) / nc.rollover + 1 : (int64_t)S.J);
     }
     const unsigned fix_y = (unsigned)std::min<int64_t>(4096, (work + 511) / 512);
-    FDSP_TRY(cuda_status(krecord(fix_ev_[li], stream)));
-    FDSP_TRY(cuda_status(kwait(fix_stream_, fix_ev_[li])));
     e = klaunch(reinterpret_cast<const void*>(tc_fix_kernel), dim3((unsigned)plan.slots.size(), fix_y), dim3(128), 0,
-                fix_stream_, L);
+                ps, L);
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     tc_groups_last_ += (int)packs[li].size();
-    if (li + 1 == plans.size()) {  // join
-      FDSP_TRY(cuda_status(krecord(fix_ev_[plans.size()], fix_stream_)));
-      FDSP_TRY(cuda_status(kwait(stream, fix_ev_[plans.size()])));
-    }
     if (done_fn_) {
       std::vector<int> egs;
       for (int gi : packs[li]) egs.push_back(gmap[gi]);
-      notify_done(egs, fix_stream_);
+      notify_done(egs, ps);
     }
+  }
+  // the side streams join the caller's stream (before the history update)
+  for (size_t si = 0; si < side_.size(); ++si) {
+    if (!side_used[si]) continue;
+    FDSP_TRY(cuda_status(krecord(pack_ev_[1 + si], side_[si])));
+    FDSP_TRY(cuda_status(kwait(stream, pack_ev_[1 + si])));
   }
   return FDSP_OK;
 }

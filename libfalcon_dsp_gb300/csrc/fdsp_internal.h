@@ -347,10 +347,10 @@ class PolyEngine {
   const float2** d_ctab_ = nullptr;    // per channel: its taps in d_ctaps_
   uint2* d_xhl_ = nullptr;             // scratch: split input of the current apply
   size_t xhl_cap_ = 0;                 // samples
-  uint8_t* d_bbuf_ = nullptr;          // scratch: B images of the current apply
-  TcLaunch* d_tcrec_ = nullptr;        // device copy of the current tensor-core launch record
-  cudaStream_t fix_stream_ = nullptr;  // exact rotation passes, beside the next packs' filter banks
-  std::vector<cudaEvent_t> fix_ev_;    // fork (one per pack) and join events
+  uint8_t* d_bbuf_ = nullptr;          // scratch: B images of the current apply (a region per launch pack)
+  TcLaunch* d_tcrec_ = nullptr;        // device copies of the launch records, one per pack (kTcMaxGroups)
+  std::vector<cudaStream_t> side_;     // launch packs 1.. (beside pack 0 on the caller's stream)
+  std::vector<cudaEvent_t> pack_ev_;   // [0]: the split is done; [1 + i]: side stream i joins
   size_t bbuf_cap_ = 0;
   int* h_err_ = nullptr;               // bounded-wait failures, mapped host memory
   int* d_err_ = nullptr;               // its device address

@@ -45,6 +45,7 @@
 namespace fdsp {
 
 constexpr int kTcMaxGroups = 16;
+constexpr int kTcSideStreams = 3;  // streams of launch packs 1.. (pack 0 runs on the caller's)
 constexpr int kTcMaxMsets = 64;
 constexpr int kTcMaxSlots = 512;
 constexpr int kTcRows = 128;           // rows per tile (MMA M)
