@@ -1112,7 +1112,9 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
     if (e != cudaSuccess) return cuda_status(e);
     launches_last_++;
     // exact pass: blocks per slot for the most rows (or rollover points) a
-    // slot of this launch has to fix
+    // slot of this launch has to fix, one per thread (the pass is latency
+    // bound: each point is a serial T-tap sum, and the last pack's pass ends
+    // the step)
     int64_t work = 1;
     for (size_t si = 0; si < plan.slots.size(); ++si) {
       const TcSlot& S = plan.slots[si];
@@ -1125,7 +1127,7 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
       const bool fast = !tc_exact_all_ && nc.rollover < 0x80000000u && 31 * Dp + S.T < (int64_t)nc.rollover;
       work = std::max<int64_t>(work, fast ? ((int64_t)S.J * Dp + S.T) / nc.rollover + 1 : (int64_t)S.J);
     }
-    const unsigned fix_y = (unsigned)std::min<int64_t>(4096, (work + 511) / 512);
+    const unsigned fix_y = (unsigned)std::min<int64_t>(4096, (work + 127) / 128);
     e = klaunch(reinterpret_cast<const void*>(tc_fix_kernel), dim3((unsigned)plan.slots.size(), fix_y), dim3(128), 0,
                 ps, L);
     if (e != cudaSuccess) return cuda_status(e);
