@@ -215,3 +215,45 @@ def test_graph_replay_matches_direct_launches(mode):
     for a, b in zip(outs[False], outs[True]):
         for ya, yb in zip(a, b):
             assert np.array_equal(ya, yb)
+
+
+@pytest.mark.parametrize("mode", ["fp16x3", "bf16x3"])
+def test_concurrent_launch_packs_match_serial_packs(mode):
+    """The 256-channel plan needs several launch packs; they run at the same
+    time on side streams (each with its own launch record and B images),
+    directly or replayed as a graph.  With kernel timing on they run one
+    after another on the caller's stream.  Every form gives bit-identical
+    outputs over a streaming sequence (state carried)."""
+    torch = pytest.importorskip("torch")
+    fs = 61440000
+    chans = channelizer_256_plan(float(fs), None, 256, 9)
+    x, _ = tone_signal(3 * 150000 + 31, float(fs), 256, seed=12)
+    xd = torch.from_numpy(x).cuda()
+    outs = {}
+    for form in ("serial", "direct", "graph"):
+        g = F.MultiRateChannelizerCuda(fs, chans)
+        g.set_precision(mode)
+        g.set_graph(form == "graph")
+        if form == "serial":
+            g.set_profile(True)
+        s = torch.cuda.Stream()
+        ys = []
+        with torch.cuda.stream(s):
+            for b in range(3):
+                n0, n1 = b * 150000, (b + 1) * 150000 + (31 if b == 2 else 0)
+                ys.append([y.clone() for y in g.apply(xd[n0:n1])])
+                if b == 0:
+                    # tensor-core form, more than one pack (3 launches a pack + history update)
+                    assert g.tc_groups() >= 2
+                    assert g.kernel_launches() >= 7
+        s.synchronize()
+        outs[form] = [[y.cpu().numpy() for y in blk] for blk in ys]
+        if form == "serial":
+            ms, n = g.read_profile()
+            assert n >= 2 * 3 and ms > 0.0
+        if form == "graph":
+            assert g.graph_replays() == 3
+    for form in ("direct", "graph"):
+        for a, b in zip(outs["serial"], outs[form]):
+            for ya, yb in zip(a, b):
+                assert np.array_equal(ya, yb), form
