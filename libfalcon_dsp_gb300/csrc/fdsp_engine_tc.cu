@@ -909,9 +909,11 @@ int PolyEngine::tc_error() {
 // pack k > 0 on side stream (k - 1) mod kTcSideStreams once the split is
 // done, and a pack's filter-bank CTAs take the SMs that the earlier packs'
 // CTAs leave as they finish (one launch's tail instead of one per pack).
-// With kernel timing on, the packs run one after another on the caller's
-// stream (each launch timed alone).  Groups no launch can hold are returned
-// in `fallback` for the FP32 kernel.
+// With kernel timing on (each launch timed alone), or with a completion hook
+// (apply_host: the first packs' device-to-host copies then start while the
+// later packs compute, where concurrent packs would all end together), the
+// packs run one after another on the caller's stream.  Groups no launch can
+// hold are returned in `fallback` for the FP32 kernel.
 int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, const std::vector<int>& tc_groups,
                           std::vector<int>& fallback, cudaStream_t stream) {
   fallback.clear();
@@ -1019,7 +1021,7 @@ int PolyEngine::launch_tc(const float2* d_in, uint64_t n, float2* const* out, co
   if (!enc) return FDSP_ERR_UNSUPPORTED;
   // (side streams and events made by build_tc, outside any stream capture)
   if (side_.empty() || pack_ev_.size() < side_.size() + 1) return FDSP_ERR_UNSUPPORTED;
-  const bool concurrent = !kprof_ && plans.size() > 1;
+  const bool concurrent = !kprof_ && !done_fn_ && plans.size() > 1;
   std::vector<char> side_used(side_.size(), 0);
   static thread_local TcLaunch L;
   for (size_t li = 0; li < plans.size(); ++li) {
