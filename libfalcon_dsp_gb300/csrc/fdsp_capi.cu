@@ -32,7 +32,7 @@ using namespace fdsp;
 struct fdsp_channelizer {
   PolyEngine eng;
   DevBuf in;
-  std::vector<DevBuf> out;
+  DevBuf arena;  // apply_host: device outputs of every channel, back to back
   // apply_host: device-to-host copies on their own stream, each group's
   // started as soon as the launches that write it are enqueued
   cudaStream_t copy = nullptr;
@@ -73,6 +73,21 @@ void channelizer_copy_back(void* ctx, const int* chans, int count, cudaStream_t 
                                        cudaMemcpyDeviceToHost, h->copy) != cudaSuccess)
       h->copy_err = 1;
   }
+}
+
+// Device outputs of an apply_host call: one allocation (grown when a block
+// needs more), channel regions back to back at 256-byte boundaries.
+int channel_arena(fdsp_channelizer* h, const std::vector<uint64_t>& cnt, std::vector<float2*>& dptr) {
+  std::vector<size_t> off(cnt.size());
+  size_t total = 0;
+  for (size_t c = 0; c < cnt.size(); ++c) {
+    off[c] = total;
+    total += (cnt[c] * sizeof(float2) + 16 + 255) & ~(size_t)255;
+  }
+  FDSP_TRY(h->arena.ensure(total + 256));
+  for (size_t c = 0; c < cnt.size(); ++c)
+    dptr[c] = reinterpret_cast<float2*>(static_cast<uint8_t*>(h->arena.p) + off[c]);
+  return FDSP_OK;
 }
 
 // apply (float or int16 input) with the outputs copied back group by group
@@ -242,7 +257,6 @@ int fdsp_channelizer_create(uint32_t fs, const fdsp_channel_cfg* ch, uint32_t nc
     delete h;
     return st;
   }
-  h->out.resize(nch);
   *out = h;
   return FDSP_OK;
 }
@@ -393,10 +407,7 @@ int fdsp_channelizer_apply_host(fdsp_channelizer* h, const fdsp_cf32* h_in, uint
   cudaStream_t s = (cudaStream_t)stream;
   FDSP_TRY(h->in.ensure(n_in * sizeof(float2) + 16));
   std::vector<float2*> dptr(nch);
-  for (uint32_t c = 0; c < nch; ++c) {
-    FDSP_TRY(h->out[c].ensure(cnt[c] * sizeof(float2) + 16));
-    dptr[c] = static_cast<float2*>(h->out[c].p);
-  }
+  FDSP_TRY(channel_arena(h, cnt, dptr));
   if (n_in) FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * sizeof(float2), cudaMemcpyHostToDevice, s)));
   FDSP_TRY(apply_with_copy_back(h, h_out, dptr.data(), n_out, s, [&] {
     return h->eng.apply(static_cast<const float2*>(h->in.p), n_in, dptr.data(), nullptr, n_out, s);
@@ -418,10 +429,7 @@ int fdsp_channelizer_apply_ci16_host(fdsp_channelizer* h, const int16_t* h_in, u
   cudaStream_t s = (cudaStream_t)stream;
   FDSP_TRY(h->in.ensure(n_in * 2 * sizeof(int16_t) + 16));
   std::vector<float2*> dptr(nch);
-  for (uint32_t c = 0; c < nch; ++c) {
-    FDSP_TRY(h->out[c].ensure(cnt[c] * sizeof(float2) + 16));
-    dptr[c] = static_cast<float2*>(h->out[c].p);
-  }
+  FDSP_TRY(channel_arena(h, cnt, dptr));
   if (n_in)
     FDSP_TRY(cuda_status(cudaMemcpyAsync(h->in.p, h_in, n_in * 2 * sizeof(int16_t), cudaMemcpyHostToDevice, s)));
   FDSP_TRY(apply_with_copy_back(h, h_out, dptr.data(), n_out, s, [&] {
@@ -869,7 +877,6 @@ int fdsp::channelizer_create_pooled(uint32_t fs, const fdsp_channel_cfg* ch, uin
     delete h;
     return st;
   }
-  h->out.resize(nch);
   *out = h;
   return FDSP_OK;
 }
