@@ -206,8 +206,10 @@ int fdsp_channelizer_set_tc_exact_all(fdsp_channelizer *h, int on);
 /* Kernel timing (diagnostics, no counterpart in the reference): while
  * enabled, applies launch directly (no graph) and each filter-bank launch
  * (tensor-core or FP32 kernel) is bracketed by CUDA events on the apply's
- * stream; enabling restarts the record.  read: synchronises and returns the
- * summed milliseconds and the number of timed launches. */
+ * stream (the tensor-core launch packs, concurrent otherwise, then run one
+ * after another on that stream); enabling restarts the record.  read:
+ * synchronises and returns the summed milliseconds and the number of timed
+ * launches. */
 int fdsp_channelizer_profile(fdsp_channelizer *h, int enable);
 int fdsp_channelizer_profile_read(fdsp_channelizer *h, double *ms, uint32_t *launches);
 /* Kernel launches the most recent apply enqueued (diagnostics, profiling). */
